@@ -1,0 +1,315 @@
+#!/usr/bin/env python
+"""SpMV benchmark: plain fp64 WPK2 `run` on the 3-D trilinear hex mesh of
+128^3 elements with 3 dofs per node (6,440,067 rows, 513,599,625 nnz).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one SpMV (engine::run) over the whole matrix.  Prints one JSON
+line (rank 0).  `value` is the algorithmic HBM throughput in GB/s
+(12 bytes per nnz + 20 bytes per row for fp64 run) with inputs resident in
+HBM; `e2e` is the same metric through the library's host-buffer call
+(H2D of x, SpMV, D2H of y every step).  The matrix (6.3 GB) is larger than
+L2, so no flush is needed between steps.
+
+--impl reference times the reference path's CPU implementation (the oracle's
+restatement of the reference's WPK2 run, OpenMP across warps) on the host
+cores for the same workload; under torchrun only rank 0 runs it.
+
+Multi-GPU: the SpMV does not shard in this build (one GPU per matrix);
+--gpus N runs N independent replicas and reports the sum of their work over
+the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SpMV HBM GB/s (% of peak) and nnz/s, fp64 plain vs fp32/bf16 at stated error"
+WORKLOAD = dict(name="hex128_3dof_fp64_wpk2_run", dim=3, e=128, dof=3, value_mode=1, seed=1)
+
+
+def alg_bytes(nrows, nnz, mapped=True):
+    """fp64 run: 8 B value + 4 B column per nnz; per row 8 B x + 8 B y (+4 B row_map)."""
+    return 12 * nnz + (20 if mapped else 16) * nrows
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic(kind, threshold):
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    return d.get(f"{kind}_t{threshold}")
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+
+    def summary(self):
+        self.f.flush()
+        rows = [ln.split(",") for ln in open(self.f.name).read().splitlines() if ln.strip()]
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 5 + i and "Active" in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def max_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_csr_baseline(rowptr, cols, vals, x, budget_s=10.0, max_reps=50):
+    """Oracle CSR multiply (OpenMP, all host threads) on the host copy of the matrix."""
+    from oracle import wk_oracle as O
+    nthreads = O.max_threads()
+    y = O.csr_spmv(rowptr, cols, vals, x, nthreads)  # warm-up (first touch of y)
+    times = []
+    t_end = time.perf_counter() + budget_s
+    while len(times) < max_reps and (not times or time.perf_counter() < t_end):
+        t0 = time.perf_counter()
+        O.lib().wko_csr_spmv_f64(rowptr, cols, vals, x, y, len(rowptr) - 1, nthreads)
+        times.append(time.perf_counter() - t0)
+    return statistics.median(times), nthreads, len(times), y
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import warpkernel_gb300 as wk
+    from warpkernel_gb300 import fe
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    W = WORKLOAD
+    rowptr, cols, vals = fe.fe_matrix(W["dim"], W["e"], W["e"], W["e"], W["dof"], W["value_mode"], W["seed"])
+    n, nnz = rowptr.numel() - 1, cols.numel()
+    x = fe.uniform_vec(W["seed"], 0, n)
+    if args.kind == 1:
+        k = wk.structure().scan(nnz, n, vals, rowptr, cols)
+    else:
+        k = wk.structure2().scan(nnz, n, vals, rowptr, cols, args.threshold)
+    eng = wk.engine(k, vals, cols)
+    y = torch.zeros(n, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    bs = args.blocksize
+    nb = (k.nwarps + bs // 32 - 1) // (bs // 32)
+
+    def step():
+        eng.run(nb, bs, x, y, cache=True, order=args.order, stream=stream, timed=False)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with Clocks(local) as clk:
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for i in range(args.steps):
+            ev[i][0].record(stream)
+            step()
+            ev[i][1].record(stream)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+    total_ms = max_over_ranks(t0.elapsed_time(t1), world)
+    kern_ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    clocks = clk.summary()
+
+    B = alg_bytes(n, nnz)
+    ms_per_step = total_ms / args.steps
+    value = world * B / (ms_per_step * 1e-3) / 1e9
+    peak, peak_kind = load_peaks()
+    achieved = B / (kern_ms * 1e-3) / 1e9
+
+    # correctness guard against the CSR product computed on the host
+    y_host = y.cpu().numpy()
+    rp_h, cols_h, vals_h, x_h = (t.cpu().numpy() for t in (rowptr, cols, vals, x))
+
+    # e2e: through the library's host-buffer call, pinned host vectors
+    xh = torch.from_numpy(x_h).pin_memory()
+    yh = torch.empty(n, dtype=torch.float64).pin_memory()
+    eng.run_host(xh, yh, mapped=True, order=args.order)
+    barrier(world)
+    te = time.perf_counter()
+    for _ in range(args.steps):
+        eng.run_host(xh, yh, mapped=True, order=args.order)
+    e2e_s = max_over_ranks((time.perf_counter() - te) / args.steps, world)
+    e2e_value = world * B / e2e_s / 1e9
+
+    out = {
+        "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(ms_per_step, 5),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded FE hex mesh generated on the device)",
+        "config": {"workload": W["name"], "mesh": "hex 128^3, 3 dof/node, random SPD element blocks",
+                   "nrows": n, "nnz": nnz, "layout": "WPK2" if args.kind == 2 else "WPK1",
+                   "threshold": args.threshold if args.kind == 2 else None, "nwarps": k.nwarps,
+                   "allocate_nz": k.allocate_nz, "order": "fast" if args.order == 0 else "exact",
+                   "blocksize": bs, "nblocks": nb, "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2 (6.3 GB matrix streamed per step), no flush"},
+        "nnz_per_s": round(world * nnz / (ms_per_step * 1e-3), 1),
+        "gflops": round(world * 2 * nnz / (ms_per_step * 1e-3) / 1e9, 2),
+        "pct_of_hbm_peak": round(100 * value / world / peak, 2),
+        "clocks": clocks,
+        "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "h2d_bytes_per_step": 8 * n,
+                "d2h_bytes_per_step": 8 * n, "ms_per_step": round(e2e_s * 1e3, 4),
+                "api": "wk_run_host (pinned host x/y)"},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                     "traffic": load_traffic(args.kind, args.threshold),
+                     "kernel": "k_spmv_fast<double,MAPPED,L1>", "kernel_ms": round(kern_ms, 5),
+                     "alg_bytes_per_launch": B},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        med, nth, reps, y_cpu = cpu_csr_baseline(rp_h, cols_h, vals_h, x_h, budget_s=args.cpu_budget)
+        out["cpu_baseline"] = {"value": round(B / med / 1e9, 2), "unit": "GB/s", "cores": nth, "kind": "port",
+                               "sample": f"full matrix, {reps} CSR multiplies (oracle wko_csr_spmv_f64, "
+                                         f"OpenMP static rows), median {med * 1e3:.2f} ms"}
+        nrm = float(np.linalg.norm(y_cpu))
+        out["rel_err_vs_host_csr"] = float(np.linalg.norm(y_host - y_cpu) / nrm) if nrm else 0.0
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return out, rank
+
+
+def run_reference(args):
+    """The reference path's arithmetic on the host cores: oracle scan + WPK
+    run in the reference's order, OpenMP across warps."""
+    import numpy as np
+
+    from oracle import wk_oracle as O
+
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return None, rank
+    W = WORKLOAD
+    rowptr, cols, vals = O.fe_matrix(W["dim"], W["e"], W["e"], W["e"], W["dof"], W["value_mode"], W["seed"])
+    n, nnz = len(rowptr) - 1, len(cols)
+    x = O.uniform_vec(W["seed"], 0, n)
+    o = O.OracleLayout(rowptr, kind=args.kind, threshold=args.threshold)
+    pv, pc = o.process(vals, cols)
+    del vals, cols
+    y = np.zeros(n)
+    nth = O.max_threads()
+    for _ in range(max(args.warmup, 3)):
+        o.run_omp(pv, pc, x, y, nth)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        o.run_omp(pv, pc, x, y, nth)
+        times.append(time.perf_counter() - t0)
+    B = alg_bytes(n, nnz)
+    ms = statistics.mean(times) * 1e3
+    value = B / (ms * 1e-3) / 1e9
+    out = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": world,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded FE hex mesh generated on the host)",
+        "config": {"workload": W["name"], "nrows": n, "nnz": nnz,
+                   "layout": "WPK2" if args.kind == 2 else "WPK1",
+                   "threshold": args.threshold if args.kind == 2 else None},
+        "nnz_per_s": round(nnz / (ms * 1e-3), 1),
+        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": nth, "kind": "port",
+                         "sample": f"full matrix per step, {args.steps} WPK run passes (oracle restatement "
+                                   "of the reference's run, OpenMP across warps)"},
+        "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's own GPU path (CUDA 4.0 texture references, sm_30) does not build with CUDA 13",
+    }
+    return out, rank
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--kind", type=int, default=2, choices=[1, 2])
+    ap.add_argument("--threshold", type=int, default=81)
+    ap.add_argument("--order", type=int, default=0, choices=[0, 1])
+    ap.add_argument("--blocksize", type=int, default=256)
+    ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        out, rank = run_reference(args)
+    else:
+        out, rank = run_ours(args)
+    if rank == 0 and out is not None:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,224 @@
+/*
+ * wk_capi.h -- C ABI of the GB300-native WPK1/WPK2 sparse matrix-vector
+ * multiply (libwarpkernel_gb300.so).
+ *
+ * This is the boundary a host binding (C++ header, ctypes, cgo, JNI ...)
+ * calls.  Signatures use plain pointers, sizes and opaque handles only.
+ * Every call returns a wk_status (0 = success) and never exits the process;
+ * wk_last_error() describes the last failure of the calling thread.
+ *
+ * Reference interface replaced: `warpkernel::structure`, `structure2` and
+ * `engine<ValueType, IndexType>` of warpkernel.hpp (thejonwong/warpkernel).
+ * Each entry point below names the reference member it stands for.
+ *
+ * Memory: pointer arguments documented as "host or device" are classified
+ * with cudaPointerGetAttributes (pageable/pinned host memory or device /
+ * managed memory of the current device).  x / y vectors of wk_run* are
+ * device pointers, as in the reference (engine::run takes device arrays).
+ *
+ * Streams: `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ * stream).  Calls are stream-ordered; only the ones that return host data or
+ * a measured time synchronise.
+ */
+#ifndef WK_CAPI_H
+#define WK_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int wk_status;
+enum {
+  WK_OK = 0,
+  WK_ERR_INVALID = 1,   /* bad argument (null pointer, size, malformed CSR ...) */
+  WK_ERR_CUDA = 2,      /* a CUDA runtime call failed */
+  WK_ERR_ALLOC = 3,     /* device or host allocation failed */
+  WK_ERR_OVERFLOW = 4,  /* layout does not fit the reference's int32 offsets */
+  WK_ERR_STATE = 5,     /* handle used in a state that does not allow the call */
+  WK_ERR_DEVICE = 6,    /* a kernel reported an error through its status word */
+  WK_ERR_NOTCONV = 7    /* an iterative solve stopped before its tolerance */
+};
+
+typedef struct wk_layout wk_layout; /* a scanned WPK1/WPK2 layout (device resident) */
+typedef struct wk_engine wk_engine; /* padded values + column indices on the device */
+
+/* Element types of values and vectors. */
+enum { WK_F64 = 0, WK_F32 = 1, WK_BF16 = 2 };
+
+/* Layout kinds: WPK1 = structure, WPK2 = structure2. */
+enum { WK_WPK1 = 1, WK_WPK2 = 2 };
+
+/* Arrays of a layout, named as the reference's public members
+ * (warpkernel.hpp:276-286, 561-562). */
+enum {
+  WK_FIELD_ROW_MAP = 0,         /* int32[nrows]     y[row_map[i]] = y'[i]          */
+  WK_FIELD_ROW_MAP_INV = 1,     /* int32[nrows]                                   */
+  WK_FIELD_REORDER_ROWS = 2,    /* uint32[nz]       new_values[reorder_rows[i]] = A[i] */
+  WK_FIELD_WARP_OFFSETS = 3,    /* int32[nwarps+1]                                */
+  WK_FIELD_MAX_NZ_ROWS = 4,     /* uint32[nwarps]                                 */
+  WK_FIELD_THREADS_PER_ROW = 5, /* uint32[nwarps]   WPK2 only                      */
+  WK_FIELD_ROW_OFFSET_WARP = 6  /* uint32[nwarps+1] WPK2 only                      */
+};
+
+typedef struct {
+  int kind;                  /* WK_WPK1 / WK_WPK2 */
+  uint32_t nrows, nznrows, nz, allocate_nz, nwarps;
+  uint32_t min_nz, max_nz;   /* WPK2: extreme non-empty row lengths */
+  uint32_t nmax_per_thread;  /* WPK2: the threshold it was scanned with */
+} wk_layout_info;
+
+/* ---- diagnostics ------------------------------------------------------- */
+
+/* Copies the calling thread's last error message (NUL-terminated, truncated
+ * to `cap`) and returns its full length.  No reference counterpart. */
+size_t wk_last_error(char *buf, size_t cap);
+/* Library version string.  No reference counterpart. */
+const char *wk_version(void);
+
+/* ---- scan (layout built on the device) ---------------------------------- */
+
+/* structure::scan(nz, nrows, A, rows, colinds) -- warpkernel.hpp:309-365.
+ * rowptr: nrows+1 CSR row offsets, host or device.  The layout arrays are
+ * built on the GPU and are bit-identical to the reference's host scan.
+ * Fails with WK_ERR_INVALID if rowptr[0] != 0, rowptr is not monotone or
+ * rowptr[nrows] != nz, and WK_ERR_OVERFLOW if allocate_nz exceeds INT32_MAX. */
+wk_status wk_scan1(const int32_t *rowptr, uint32_t nrows, uint32_t nz, void *stream,
+                   wk_layout **out);
+
+/* structure2::scan(nz, nrows, A, rows, colinds, threshold) --
+ * warpkernel.hpp:579-736.  Same inputs plus the per-thread threshold. */
+wk_status wk_scan2(const int32_t *rowptr, uint32_t nrows, uint32_t nz, int32_t threshold,
+                   void *stream, wk_layout **out);
+
+wk_status wk_layout_info_get(const wk_layout *l, wk_layout_info *info);
+
+/* Copies one layout array to host memory.  `dst` may be NULL to query the
+ * element count in *count; otherwise `cap` is its capacity in elements. */
+wk_status wk_layout_get(const wk_layout *l, int field, void *dst, size_t cap, size_t *count);
+
+/* Releases the caller's reference; device memory is freed when no engine
+ * created from the layout remains. */
+wk_status wk_layout_destroy(wk_layout *l);
+
+/* ---- reorderings -------------------------------------------------------- */
+
+/* structure::reorder_columns_coalesced(colinds) -- warpkernel.hpp:447-457.
+ * cols: nz CSR column indices (host or device); out: allocate_nz padded,
+ * renumbered column indices (host or device).  Padding slots are 0. */
+wk_status wk_reorder_columns_coalesced(const wk_layout *l, const int32_t *cols, int32_t *out,
+                                       void *stream);
+
+/* structure::reorder_columns(colinds) -- warpkernel.hpp:401-412: nz column
+ * indices renumbered to sorted order, CSR order kept. */
+wk_status wk_reorder_columns(const wk_layout *l, const int32_t *cols, int32_t *out, void *stream);
+
+/* structure::reorder_x(x, device_x) -- warpkernel.hpp:518-530:
+ * x_out[row_map_inv[r]] = x[r].  dtype WK_F64 / WK_F32 / WK_BF16. */
+wk_status wk_reorder_x(const wk_layout *l, int dtype, const void *x, void *x_out, void *stream);
+
+/* ---- engine ------------------------------------------------------------- */
+
+/* engine(structure&, A, colinds) / engine(structure2&, A, colinds), which
+ * call structure::process -- warpkernel.hpp:794-809, 533-548, 750-769.
+ * vals: nz values of type `dtype`, cols: nz column indices (each host or
+ * device).  The padded, interleaved arrays are built on the GPU.  ncols is
+ * the length of x (every column index must lie in [0, ncols)).  The engine
+ * keeps the layout alive. */
+wk_status wk_engine_create(wk_layout *l, int dtype, const void *vals, const int32_t *cols,
+                           uint32_t ncols, void *stream, wk_engine **out);
+
+/* Replaces the engine's padded column indices by caller-supplied ones
+ * (allocate_nz entries, host or device), e.g. the output of
+ * wk_reorder_columns_coalesced -- the reference drivers assign
+ * `eng.device_colinds = reorder_cols` (wpk1.cu:175, 198).  Indices are
+ * validated against ncols. */
+wk_status wk_engine_set_colinds(wk_engine *e, const int32_t *padded_cols, void *stream);
+
+/* Replaces the engine's values from CSR-ordered `vals` (nz entries, host or
+ * device, of the engine's dtype) without rescanning -- reference process()
+ * with the same structure. */
+wk_status wk_engine_set_values(wk_engine *e, const void *vals, void *stream);
+
+/* Copies engine.device_values / device_colinds (allocate_nz entries) out. */
+wk_status wk_engine_get_values(const wk_engine *e, void *dst, size_t cap);
+wk_status wk_engine_get_colinds(const wk_engine *e, int32_t *dst, size_t cap);
+
+wk_status wk_engine_destroy(wk_engine *e);
+
+/* ---- SpMV --------------------------------------------------------------- */
+
+/* Accumulation order of wk_run / wk_run_x. */
+enum {
+  WK_ORDER_FAST = 0,  /* 256/128-bit loads; each lane's slots re-associated */
+  WK_ORDER_EXACT = 1  /* the reference's order, bit-identical to the oracle  */
+};
+
+/* engine::run<cache>(nblocks, blocksize, dx, dy) -- warpkernel.hpp:811-860:
+ * y[row_map[p]] = sum over row p.  dx: ncols device values, dy: nrows device
+ * values of the engine's dtype (FP32 accumulation and FP32 y for WK_BF16
+ * engines).  blocksize: threads per block (a multiple of 32, <= 1024);
+ * nblocks must cover nwarps / (blocksize/32) blocks; nblocks <= 0 or
+ * blocksize <= 0 selects the launch shape automatically.  cache != 0 gathers
+ * x through L1 (the texture-cache path of the reference), 0 through L2 only.
+ * If `seconds` is non-NULL the call synchronises and stores the kernel time
+ * measured with CUDA events (the reference returns elapsed seconds);
+ * otherwise it returns right after the launch.  Rows without entries are not
+ * written. */
+wk_status wk_run(wk_engine *e, int nblocks, int blocksize, int cache, int order, const void *dx,
+                 void *dy, void *stream, float *seconds);
+
+/* engine::run_x<cache>(...) -- warpkernel.hpp:862-896: y'[p] = sum over
+ * sorted row p (no row_map scatter).  Used with renumbered columns and the
+ * reordered x of wk_reorder_x. */
+wk_status wk_run_x(wk_engine *e, int nblocks, int blocksize, int cache, int order, const void *dx,
+                   void *dy, void *stream, float *seconds);
+
+/* engine::run with HOST vectors: copies x_host (ncols values) to an
+ * engine-owned device buffer, runs the SpMV and copies y back into y_host
+ * (nrows values; entries of empty rows are written as 0).  This is the
+ * reference drivers' sequence (H2D of x, run, D2H of y: wpk1.cu:120, 149,
+ * 155) in one call.  `mapped` 1 = run, 0 = run_x.  Pinned host buffers give
+ * the fastest copies.  Synchronous. */
+wk_status wk_run_host(wk_engine *e, int mapped, int order, const void *x_host, void *y_host,
+                      void *stream);
+
+/* ---- verification ------------------------------------------------------- */
+
+/* engine::verify(orig, comp) -- warpkernel.hpp:932-943 (host arrays of nrows
+ * doubles; 1e-5 relative, 1e-14 absolute for |orig| <= 1e-14).  *pass = 1 if
+ * it passes; *first_bad = first failing index or -1. */
+wk_status wk_verify(const wk_layout *l, const double *orig, const double *comp, int *pass,
+                    int64_t *first_bad);
+
+/* engine::verify_x(orig, comp) -- warpkernel.hpp:945-957.  strict = 0 keeps
+ * the reference's condition exactly (it mixes orig[row_map[i]] and orig[i]);
+ * strict = 1 uses orig[row_map[i]] throughout. */
+wk_status wk_verify_x(const wk_layout *l, const double *orig, const double *comp, int strict,
+                      int *pass, int64_t *first_bad);
+
+/* ---- device and test-input utilities (no reference counterpart) --------- */
+
+/* Finite-element test matrix generated on the device (same numbering and
+ * bit-identical values as the CPU generator used by the tests).
+ * dim 2: ex x ey Q1 quads; dim 3: ex x ey x ez hexes; dof unknowns per node.
+ * value_mode 0: off-diagonal U(-1,0) symmetric, diagonal 1.01 x absolute row
+ * sum; 1: assembled random SPD element blocks scaled by the element volume.
+ * wk_fe_size gives the sizes; wk_fe_fill writes device arrays rowptr
+ * (nrows+1), cols (nnz) and vals (nnz, float64); any may be NULL. */
+wk_status wk_fe_size(int dim, int ex, int ey, int ez, int dof, int64_t *nrows, int64_t *nnz);
+wk_status wk_fe_fill(int dim, int ex, int ey, int ez, int dof, int value_mode, uint64_t seed,
+                     int32_t *rowptr, int32_t *cols, double *vals, void *stream);
+/* Uniform(-1,1) float64 device vector from the generator's hash. */
+wk_status wk_uniform_vec(uint64_t seed, uint64_t stream_id, double *x, int64_t n, void *stream);
+/* Element-type conversion of a device vector (float64 -> float32/bf16 with
+ * round-to-nearest-even, or back). */
+wk_status wk_convert(const void *src, int src_dtype, void *dst, int dst_dtype, int64_t n,
+                     void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WK_CAPI_H */

@@ -1,0 +1,197 @@
+"""engine::run / run_x on the GPU against the reference's own WPK1 kernel
+outputs (golden), the oracle's documented order, and size-independent
+properties at full size."""
+import numpy as np
+import pytest
+
+from conftest import golden_cases, random_csr
+from oracle import wk_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL_FAST = 1e-12  # normwise relative, fp64, re-associated order
+
+
+def wk():
+    import warpkernel_gb300
+    return warpkernel_gb300
+
+
+def torch():
+    import torch as t
+    return t
+
+
+def make(kind, rp, cols, vals, th=0, dtype="f64"):
+    k = wk().structure() if kind == 1 else wk().structure2()
+    if kind == 1:
+        k.scan(len(cols), len(rp) - 1, vals, rp, cols)
+    else:
+        k.scan(len(cols), len(rp) - 1, vals, rp, cols, th)
+    v = vals if dtype == "f64" else vals.astype(np.float32)
+    return k, wk().engine(k, v, cols, dtype=dtype)
+
+
+def run(eng, x, mapped=True, order=0, cache=True, nblocks=0, blocksize=256, y0=0.0):
+    t = torch()
+    n = eng.kernel.nrows
+    dx = t.from_numpy(np.ascontiguousarray(x)).cuda()
+    dy = t.full((n,), y0, dtype=dx.dtype, device="cuda")
+    f = eng.run if mapped else eng.run_x
+    sec = f(nblocks, blocksize, dx, dy, cache=cache, order=order)
+    assert sec >= 0
+    return dy.cpu().numpy()
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.int64)
+
+
+def relerr(y, ref):
+    d = np.linalg.norm(ref)
+    return np.linalg.norm(y - ref) / (d if d else 1.0)
+
+
+def test_wpk1_matches_reference_kernel_outputs(golden):
+    """Exact order is bit-identical to the reference's warpKernel /
+    warpKernel_reorderx compiled with contraction (golden y_run_fma)."""
+    for name, rp, cols, vals, x, layouts in golden_cases(golden):
+        tag = f"{name}/k1_t0"
+        if f"{tag}/y_run_fma" not in golden:
+            continue
+        k, eng = make(1, rp, cols, vals)
+        y = run(eng, x, order=wk().WK_ORDER_EXACT)
+        assert np.array_equal(bits(y), bits(golden[f"{tag}/y_run_fma"])), tag
+        y = run(eng, x)
+        assert relerr(y, golden[f"{tag}/y_run_fma"]) < REL_TOL_FAST, tag
+        eng.device_colinds = golden[f"{tag}/pcols_renum"]
+        xr = golden[f"{tag}/x_reordered"]
+        y = run(eng, xr, mapped=False, order=wk().WK_ORDER_EXACT)
+        assert np.array_equal(bits(y), bits(golden[f"{tag}/y_runx_fma"])), tag
+        y = run(eng, xr, mapped=False)
+        assert relerr(y, golden[f"{tag}/y_runx_fma"]) < REL_TOL_FAST, tag
+
+
+def check_all_variants(rp, cols, vals, x, kind, th, tag, shapes=((0, 256),)):
+    k, eng = make(kind, rp, cols, vals, th)
+    with O.OracleLayout(rp, kind=kind, threshold=th) as o:
+        pv, pc = o.process(vals, cols)
+        y_ref = o.run(pv, pc, x, fma=True)
+        pcr = o.reorder_columns_coalesced(cols)
+        xr = o.reorder_x(x)
+        yx_ref = o.run_x(pv, pcr, xr, fma=True)
+    for nblocks, bs in shapes:
+        for cache in (True, False):
+            y = run(eng, x, order=1, cache=cache, nblocks=nblocks, blocksize=bs)
+            assert np.array_equal(bits(y), bits(y_ref)), (tag, "exact", bs, cache)
+            y = run(eng, x, order=0, cache=cache, nblocks=nblocks, blocksize=bs)
+            assert relerr(y, y_ref) < REL_TOL_FAST, (tag, "fast", bs, cache, relerr(y, y_ref))
+    # WPK_r (run_x) and WPK_rx (run with renumbered columns and reordered x)
+    eng.device_colinds = k.reorder_columns_coalesced(cols)
+    y = run(eng, xr, mapped=False, order=1)
+    assert np.array_equal(bits(y), bits(yx_ref)), (tag, "run_x exact")
+    y = run(eng, xr, mapped=False)
+    assert relerr(y, yx_ref) < REL_TOL_FAST, (tag, "run_x fast")
+    assert eng.verify_x(y_ref, y)
+    y = run(eng, xr, mapped=True)
+    assert relerr(y, y_ref) < REL_TOL_FAST, (tag, "rx fast")
+    assert eng.verify(y_ref, y)
+
+
+def test_golden_layouts_all_variants(golden):
+    for name, rp, cols, vals, x, layouts in golden_cases(golden):
+        if len(cols) == 0:
+            continue
+        for kind, th in layouts:
+            check_all_variants(rp, cols, vals, x, kind, th, f"{name}/{kind}/{th}",
+                               shapes=((0, 32), (0, 256), (0, 1024), (10000, 64)))
+
+
+def test_random_matrices():
+    rng = np.random.default_rng(17)
+    for trial in range(25):
+        n = int(rng.integers(2, 5000))
+        rp, cols, vals = random_csr(rng, n, int(rng.choice([3, 9, 27, 81, 300])), float(rng.choice([0, 0.2])))
+        if len(cols) == 0:
+            continue
+        x = rng.uniform(-1, 1, n)
+        for kind, th in ((1, 0), (2, int(rng.integers(0, 40)))):
+            check_all_variants(rp, cols, vals, x, kind, th, (trial, kind, th))
+
+
+def test_config1_q1_128_threshold_sweep():
+    """2-D Q1 128x128, 1 dof (16,641 rows): WPK1 and the WPK2 threshold sweep
+    of the reference's wpk2 driver (min_nz..max_nz, 10% steps), every
+    warps-per-block of the drivers."""
+    rp, cols, vals = O.fe_matrix(2, 128, 128, 0, 1, value_mode=0, seed=0)
+    x = O.uniform_vec(0, 0, len(rp) - 1)
+    check_all_variants(rp, cols, vals, x, 1, 0, "c1 wpk1",
+                       shapes=tuple((0, 32 * w) for w in range(1, 17)))
+    k2 = wk().structure2().scan(len(cols), len(rp) - 1, vals, rp, cols, len(rp) - 1)
+    lo, hi = k2.min_nz, k2.max_nz
+    assert (lo, hi) == (4, 9)
+    inc = max(int((hi - lo) * 0.1), 1)
+    for th in range(lo, hi + 1, inc):
+        check_all_variants(rp, cols, vals, x, 2, th, f"c1 wpk2 th={th}",
+                           shapes=tuple((0, 32 * w) for w in (2, 4, 8, 16)))
+
+
+def test_empty_rows_are_not_written():
+    rp = np.array([0, 2, 2, 3, 3], np.int32)
+    cols = np.array([0, 3, 1], np.int32)
+    vals = np.array([1.0, 2.0, 3.0])
+    x = np.array([1.0, 2.0, 3.0, 4.0])
+    for kind in (1, 2):
+        _, eng = make(kind, rp, cols, vals, 1)
+        for order in (0, 1):
+            y = run(eng, x, order=order, y0=-7.0)
+            assert list(y) == [9.0, -7.0, 6.0, -7.0]
+
+
+def test_launch_shape_checks():
+    rng = np.random.default_rng(1)
+    rp, cols, vals = random_csr(rng, 2000, 9)
+    k, eng = make(1, rp, cols, vals)
+    t = torch()
+    dx = t.ones(2000, dtype=t.float64, device="cuda")
+    dy = t.zeros(2000, dtype=t.float64, device="cuda")
+    with pytest.raises(wk().WKError, match="nblocks"):
+        eng.run(1, 64, dx, dy)
+    with pytest.raises(wk().WKError, match="blocksize"):
+        eng.run(1000, 48, dx, dy)
+    nb = (k.nwarps + 3) // 4
+    eng.run(nb, 128, dx, dy)  # the drivers' exact grid is accepted
+
+
+def test_mixed_precision_error_bounds():
+    rp, cols, vals = O.fe_matrix(3, 12, 12, 12, 3, value_mode=1, seed=2)
+    n = len(rp) - 1
+    x = O.uniform_vec(2, 0, n)
+    y64 = O.csr_spmv(rp, cols, vals, x)
+    t = torch()
+    for dtype, tol in (("f32", 1e-6), ("bf16", 1e-2)):
+        for kind, th in ((1, 0), (2, 27)):
+            k = wk().structure() if kind == 1 else wk().structure2()
+            k.scan(len(cols), n, None, rp, None, *(() if kind == 1 else (th,)))
+            tv = t.from_numpy(vals).cuda()
+            tdt = t.float32 if dtype == "f32" else t.bfloat16
+            eng = wk().engine(k, wk().fe.convert(tv, tdt), t.from_numpy(cols).cuda(), dtype=dtype)
+            dx = wk().fe.convert(t.from_numpy(x).cuda(), tdt)
+            dy = t.zeros(n, dtype=t.float32, device="cuda")
+            for order in (0, 1):
+                eng.run(0, 256, dx, dy, order=order)
+                err = relerr(dy.double().cpu().numpy(), y64)
+                assert err < tol, (dtype, kind, order, err)
+
+
+def test_device_generator_matches_cpu_generator():
+    t = torch()
+    for args, mode in (((2, 20, 17, 0, 1), 0), ((3, 5, 4, 3, 3), 1), ((2, 6, 6, 0, 2), 1), ((3, 2, 2, 2, 1), 0)):
+        rp, cols, vals = O.fe_matrix(*args, value_mode=mode, seed=5)
+        drp, dcols, dvals = wk().fe.fe_matrix(*args, value_mode=mode, seed=5)
+        assert np.array_equal(drp.cpu().numpy(), rp)
+        assert np.array_equal(dcols.cpu().numpy(), cols)
+        assert np.array_equal(bits(dvals.cpu().numpy()), bits(vals)), args
+    x = O.uniform_vec(3, 1, 1000)
+    assert np.array_equal(bits(wk().fe.uniform_vec(3, 1, 1000).cpu().numpy()), bits(x))
+    assert t.cuda.is_available()

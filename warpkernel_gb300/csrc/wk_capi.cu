@@ -1,0 +1,476 @@
+// wk_capi.cu -- the C ABI (include/wk_capi.h): argument checks, handle
+// lifetime, host/device classification of caller pointers, verify.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "wk_internal.cuh"
+
+namespace wk {
+
+namespace {
+thread_local std::string g_err;
+}
+
+wk_status set_error(wk_status code, const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+const std::string &last_error() { return g_err; }
+
+bool is_device_ptr(const void *ptr) {
+  if (!ptr) return false;
+  cudaPointerAttributes at;
+  cudaError_t e = cudaPointerGetAttributes(&at, ptr);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+wk_status DevView::from(const void *src, size_t bytes, cudaStream_t st) {
+  if (is_device_ptr(src)) {
+    dptr = src;
+    return WK_OK;
+  }
+  WK_TRY(tmp.alloc(bytes));
+  if (bytes) WK_CUDA(cudaMemcpyAsync(tmp.p, src, bytes, cudaMemcpyHostToDevice, st));
+  dptr = tmp.p;
+  return WK_OK;
+}
+
+wk_status copy_out(void *dst, const void *src, size_t bytes, cudaStream_t st) {
+  if (!bytes) return WK_OK;
+  WK_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, st));
+  return WK_OK;
+}
+
+size_t dtype_size(int dtype) {
+  switch (dtype) {
+    case WK_F64: return 8;
+    case WK_F32: return 4;
+    case WK_BF16: return 2;
+  }
+  return 0;
+}
+
+}  // namespace wk
+
+using namespace wk;
+
+namespace {
+
+cudaStream_t S(void *stream) { return (cudaStream_t)stream; }
+
+void layout_release(wk_layout *l) {
+  if (l && l->refs.fetch_sub(1) == 1) {
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(l->device);
+    delete l;  // DevBufs free on the layout's device
+    cudaSetDevice(prev);
+  }
+}
+
+// Renumbering through row_map_inv needs every column index in [0, nrows).
+wk_status check_square_cols(const wk_layout *l, const int32_t *dcols, cudaStream_t st) {
+  DevBuf bad;
+  WK_TRY(bad.alloc(sizeof(int)));
+  WK_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), st));
+  WK_TRY(launch_check_cols(dcols, l->info.nz, l->info.nrows, bad.as<int>(), st));
+  int h = 0;
+  WK_CUDA(cudaMemcpyAsync(&h, bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  WK_CUDA(cudaStreamSynchronize(st));
+  if (h) return set_error(WK_ERR_INVALID, "%d column indices lie outside [0, nrows = %u)", h, l->info.nrows);
+  return WK_OK;
+}
+
+wk_status scan_common(const int32_t *rowptr, uint32_t nrows, uint32_t nz, int kind, int32_t th,
+                      void *stream, wk_layout **out) {
+  if (!out) return set_error(WK_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  if (!rowptr) return set_error(WK_ERR_INVALID, "rowptr is NULL");
+  if (nrows > 0x7fffffffu) return set_error(WK_ERR_INVALID, "nrows %u exceeds INT32_MAX", nrows);
+  if (nz > 0x7fffffffu) return set_error(WK_ERR_INVALID, "nz %u exceeds INT32_MAX", nz);
+  if (!is_device_ptr(rowptr)) {  // host input: reject malformed CSR before any device work
+    if (rowptr[0] != 0) return set_error(WK_ERR_INVALID, "rowptr[0] = %d, expected 0", rowptr[0]);
+    for (uint32_t r = 0; r < nrows; r++)
+      if (rowptr[r + 1] < rowptr[r]) return set_error(WK_ERR_INVALID, "rowptr is not monotone at row %u", r);
+    if ((uint32_t)rowptr[nrows] != nz)
+      return set_error(WK_ERR_INVALID, "rowptr[nrows] = %d does not equal nz = %u", rowptr[nrows], nz);
+  }
+  wk_layout *l = new (std::nothrow) wk_layout();
+  if (!l) return set_error(WK_ERR_ALLOC, "host allocation failed");
+  cudaGetDevice(&l->device);
+  l->info.nrows = nrows;
+  l->info.nz = nz;
+  cudaStream_t st = S(stream);
+  wk_status s = l->bufs[7].alloc(((size_t)nrows + 1) * 4);
+  if (s == WK_OK) {
+    cudaError_t e = cudaMemcpyAsync(l->bufs[7].p, rowptr, ((size_t)nrows + 1) * 4, cudaMemcpyDefault, st);
+    if (e != cudaSuccess) s = set_error(WK_ERR_CUDA, "rowptr copy failed: %s", cudaGetErrorString(e));
+  }
+  if (s == WK_OK) s = build_layout(l, l->bufs[7].as<int32_t>(), kind, th, st);
+  if (s != WK_OK) {
+    delete l;
+    return s;
+  }
+  *out = l;
+  return WK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t wk_last_error(char *buf, size_t cap) {
+  const std::string &e = last_error();
+  if (buf && cap) {
+    size_t n = e.size() < cap - 1 ? e.size() : cap - 1;
+    memcpy(buf, e.data(), n);
+    buf[n] = 0;
+  }
+  return e.size();
+}
+
+const char *wk_version(void) { return "warpkernel_gb300 0.1 (sm_103a)"; }
+
+wk_status wk_scan1(const int32_t *rowptr, uint32_t nrows, uint32_t nz, void *stream, wk_layout **out) {
+  return scan_common(rowptr, nrows, nz, WK_WPK1, 0, stream, out);
+}
+
+wk_status wk_scan2(const int32_t *rowptr, uint32_t nrows, uint32_t nz, int32_t threshold, void *stream,
+                   wk_layout **out) {
+  return scan_common(rowptr, nrows, nz, WK_WPK2, threshold, stream, out);
+}
+
+wk_status wk_layout_info_get(const wk_layout *l, wk_layout_info *info) {
+  if (!l || !info) return set_error(WK_ERR_INVALID, "NULL argument");
+  *info = l->info;
+  return WK_OK;
+}
+
+wk_status wk_layout_get(const wk_layout *l, int field, void *dst, size_t cap, size_t *count) {
+  if (!l) return set_error(WK_ERR_INVALID, "layout is NULL");
+  const wk_layout_info &I = l->info;
+  const void *src = nullptr;
+  size_t n = 0;
+  const bool k2 = I.kind == WK_WPK2;
+  switch (field) {
+    case WK_FIELD_ROW_MAP: src = l->d.row_map; n = I.nrows; break;
+    case WK_FIELD_ROW_MAP_INV: src = l->d.row_map_inv; n = I.nrows; break;
+    case WK_FIELD_REORDER_ROWS: src = l->d.reorder_rows; n = I.nz; break;
+    case WK_FIELD_WARP_OFFSETS: src = l->d.warp_offsets; n = (size_t)I.nwarps + 1; break;
+    case WK_FIELD_MAX_NZ_ROWS: src = l->d.max_nz_rows; n = I.nwarps; break;
+    case WK_FIELD_THREADS_PER_ROW: src = l->d.threads_per_row; n = k2 ? I.nwarps : 0; break;
+    case WK_FIELD_ROW_OFFSET_WARP: src = l->d.row_offset_warp; n = k2 ? (size_t)I.nwarps + 1 : 0; break;
+    default: return set_error(WK_ERR_INVALID, "unknown field %d", field);
+  }
+  if (count) *count = n;
+  if (!dst) return WK_OK;
+  if (cap < n) return set_error(WK_ERR_INVALID, "capacity %zu < %zu elements", cap, n);
+  if (n) {
+    WK_CUDA(cudaMemcpy(dst, src, n * 4, cudaMemcpyDefault));
+  }
+  return WK_OK;
+}
+
+wk_status wk_layout_destroy(wk_layout *l) {
+  layout_release(l);
+  return WK_OK;
+}
+
+wk_status wk_reorder_columns_coalesced(const wk_layout *l, const int32_t *cols, int32_t *out, void *stream) {
+  if (!l || !cols || !out) return set_error(WK_ERR_INVALID, "NULL argument");
+  cudaStream_t st = S(stream);
+  DevView c;
+  WK_TRY(c.from(cols, (size_t)l->info.nz * 4, st));
+  WK_TRY(check_square_cols(l, (const int32_t *)c.dptr, st));
+  bool dev_out = is_device_ptr(out);
+  DevBuf tmp;
+  int32_t *dout = out;
+  if (!dev_out) {
+    WK_TRY(tmp.alloc((size_t)l->info.allocate_nz * 4));
+    dout = tmp.as<int32_t>();
+  }
+  if (l->info.allocate_nz && l->info.nwarps == 0)
+    return set_error(WK_ERR_STATE, "inconsistent layout");
+  WK_TRY(launch_process(l, nullptr, 8, (const int32_t *)c.dptr, nullptr, dout, true, st));
+  if (!dev_out) WK_TRY(copy_out(out, dout, (size_t)l->info.allocate_nz * 4, st));
+  WK_CUDA(cudaStreamSynchronize(st));
+  return WK_OK;
+}
+
+wk_status wk_reorder_columns(const wk_layout *l, const int32_t *cols, int32_t *out, void *stream) {
+  if (!l || !cols || !out) return set_error(WK_ERR_INVALID, "NULL argument");
+  cudaStream_t st = S(stream);
+  DevView c;
+  WK_TRY(c.from(cols, (size_t)l->info.nz * 4, st));
+  WK_TRY(check_square_cols(l, (const int32_t *)c.dptr, st));
+  bool dev_out = is_device_ptr(out);
+  DevBuf tmp;
+  int32_t *dout = out;
+  if (!dev_out) {
+    WK_TRY(tmp.alloc((size_t)l->info.nz * 4));
+    dout = tmp.as<int32_t>();
+  }
+  WK_TRY(launch_reorder_columns(l, (const int32_t *)c.dptr, dout, st));
+  if (!dev_out) WK_TRY(copy_out(out, dout, (size_t)l->info.nz * 4, st));
+  WK_CUDA(cudaStreamSynchronize(st));
+  return WK_OK;
+}
+
+wk_status wk_reorder_x(const wk_layout *l, int dtype, const void *x, void *x_out, void *stream) {
+  if (!l || !x || !x_out) return set_error(WK_ERR_INVALID, "NULL argument");
+  size_t eb = dtype_size(dtype);
+  if (!eb) return set_error(WK_ERR_INVALID, "unknown dtype %d", dtype);
+  cudaStream_t st = S(stream);
+  size_t bytes = (size_t)l->info.nrows * eb;
+  DevView xv;
+  WK_TRY(xv.from(x, bytes, st));
+  bool dev_out = is_device_ptr(x_out);
+  DevBuf tmp;
+  void *dout = x_out;
+  if (!dev_out) {
+    WK_TRY(tmp.alloc(bytes));
+    dout = tmp.p;
+  }
+  WK_TRY(launch_reorder_x(l, xv.dptr, dout, (int)eb, st));
+  if (!dev_out) {
+    WK_TRY(copy_out(x_out, dout, bytes, st));
+    WK_CUDA(cudaStreamSynchronize(st));
+  } else if (xv.tmp.p) {
+    WK_CUDA(cudaStreamSynchronize(st));
+  }
+  return WK_OK;
+}
+
+wk_status wk_engine_create(wk_layout *l, int dtype, const void *vals, const int32_t *cols, uint32_t ncols,
+                           void *stream, wk_engine **out) {
+  if (!out) return set_error(WK_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  if (!l || !vals || !cols) return set_error(WK_ERR_INVALID, "NULL argument");
+  size_t eb = dtype_size(dtype);
+  if (!eb) return set_error(WK_ERR_INVALID, "unknown dtype %d", dtype);
+  if (ncols == 0 && l->info.nz) return set_error(WK_ERR_INVALID, "ncols is 0 but the matrix has entries");
+  cudaStream_t st = S(stream);
+  wk_engine *e = new (std::nothrow) wk_engine();
+  if (!e) return set_error(WK_ERR_ALLOC, "host allocation failed");
+  e->dtype = dtype;
+  e->ncols = ncols;
+  const size_t anz = l->info.allocate_nz, nz = l->info.nz;
+  wk_status s = WK_OK;
+  DevView v, c;
+  if (s == WK_OK) s = v.from(vals, nz * eb, st);
+  if (s == WK_OK) s = c.from(cols, nz * 4, st);
+  if (s == WK_OK) s = e->vals.alloc(anz * eb);
+  if (s == WK_OK) s = e->cols.alloc(anz * 4);
+  if (s == WK_OK) s = e->status.alloc(64);
+  int bad = 0;
+  if (s == WK_OK) {
+    cudaMemsetAsync(e->status.p, 0, 64, st);
+    s = launch_check_cols((const int32_t *)c.dptr, nz, ncols, e->status.as<int>(), st);
+  }
+  if (s == WK_OK) s = launch_process(l, v.dptr, (int)eb, (const int32_t *)c.dptr, e->vals.p,
+                                     e->cols.as<int32_t>(), false, st);
+  if (s == WK_OK) {
+    cudaError_t ce = cudaMemcpyAsync(&bad, e->status.p, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (ce != cudaSuccess) s = set_error(WK_ERR_CUDA, "engine creation: %s", cudaGetErrorString(ce));
+  }
+  if (s == WK_OK && bad)
+    s = set_error(WK_ERR_INVALID, "%d column indices lie outside [0, %u)", bad, ncols);
+  if (s != WK_OK) {
+    delete e;
+    return s;
+  }
+  l->refs.fetch_add(1);
+  e->layout = l;
+  *out = e;
+  return WK_OK;
+}
+
+wk_status wk_engine_set_colinds(wk_engine *e, const int32_t *padded_cols, void *stream) {
+  if (!e || !padded_cols) return set_error(WK_ERR_INVALID, "NULL argument");
+  cudaStream_t st = S(stream);
+  const size_t anz = e->layout->info.allocate_nz;
+  DevView c;
+  WK_TRY(c.from(padded_cols, anz * 4, st));
+  WK_CUDA(cudaMemsetAsync(e->status.p, 0, sizeof(int), st));
+  WK_TRY(launch_check_cols((const int32_t *)c.dptr, anz, e->ncols, e->status.as<int>(), st));
+  int bad = 0;
+  WK_CUDA(cudaMemcpyAsync(&bad, e->status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  WK_CUDA(cudaStreamSynchronize(st));
+  if (bad) return set_error(WK_ERR_INVALID, "%d column indices lie outside [0, %u)", bad, e->ncols);
+  if (anz) WK_CUDA(cudaMemcpyAsync(e->cols.p, c.dptr, anz * 4, cudaMemcpyDeviceToDevice, st));
+  WK_CUDA(cudaStreamSynchronize(st));
+  return WK_OK;
+}
+
+wk_status wk_engine_set_values(wk_engine *e, const void *vals, void *stream) {
+  if (!e || !vals) return set_error(WK_ERR_INVALID, "NULL argument");
+  cudaStream_t st = S(stream);
+  const size_t eb = dtype_size(e->dtype);
+  DevView v;
+  WK_TRY(v.from(vals, (size_t)e->layout->info.nz * eb, st));
+  WK_TRY(launch_process(e->layout, v.dptr, (int)eb, nullptr, e->vals.p, nullptr, false, st));
+  if (v.tmp.p) WK_CUDA(cudaStreamSynchronize(st));
+  return WK_OK;
+}
+
+wk_status wk_engine_get_values(const wk_engine *e, void *dst, size_t cap) {
+  if (!e || !dst) return set_error(WK_ERR_INVALID, "NULL argument");
+  size_t n = e->layout->info.allocate_nz;
+  if (cap < n) return set_error(WK_ERR_INVALID, "capacity %zu < %zu", cap, n);
+  if (n) WK_CUDA(cudaMemcpy(dst, e->vals.p, n * dtype_size(e->dtype), cudaMemcpyDefault));
+  return WK_OK;
+}
+
+wk_status wk_engine_get_colinds(const wk_engine *e, int32_t *dst, size_t cap) {
+  if (!e || !dst) return set_error(WK_ERR_INVALID, "NULL argument");
+  size_t n = e->layout->info.allocate_nz;
+  if (cap < n) return set_error(WK_ERR_INVALID, "capacity %zu < %zu", cap, n);
+  if (n) WK_CUDA(cudaMemcpy(dst, e->cols.p, n * 4, cudaMemcpyDefault));
+  return WK_OK;
+}
+
+wk_status wk_engine_destroy(wk_engine *e) {
+  if (!e) return WK_OK;
+  wk_layout *l = e->layout;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  if (l) cudaSetDevice(l->device);
+  delete e;
+  cudaSetDevice(prev);
+  layout_release(l);
+  return WK_OK;
+}
+
+static wk_status run_common(wk_engine *e, int nblocks, int blocksize, int cache, int order, const void *dx,
+                            void *dy, void *stream, float *seconds, bool mapped) {
+  if (!e || !dx || !dy) return set_error(WK_ERR_INVALID, "NULL argument");
+  if (order != WK_ORDER_FAST && order != WK_ORDER_EXACT)
+    return set_error(WK_ERR_INVALID, "unknown order %d", order);
+  cudaStream_t st = S(stream);
+  RunArgs a{e, nblocks, blocksize, cache, order, mapped, dx, dy, st};
+  if (!seconds) return launch_spmv(a);
+  cudaEvent_t t0, t1;
+  WK_CUDA(cudaEventCreate(&t0));
+  WK_CUDA(cudaEventCreate(&t1));
+  cudaEventRecord(t0, st);
+  wk_status s = launch_spmv(a);
+  cudaEventRecord(t1, st);
+  cudaError_t ce = cudaEventSynchronize(t1);
+  float ms = 0.f;
+  if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, t0, t1);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  if (s != WK_OK) return s;
+  if (ce != cudaSuccess) return set_error(WK_ERR_CUDA, "run: %s", cudaGetErrorString(ce));
+  *seconds = ms * 1e-3f;
+  return WK_OK;
+}
+
+wk_status wk_run(wk_engine *e, int nblocks, int blocksize, int cache, int order, const void *dx, void *dy,
+                 void *stream, float *seconds) {
+  return run_common(e, nblocks, blocksize, cache, order, dx, dy, stream, seconds, true);
+}
+
+wk_status wk_run_x(wk_engine *e, int nblocks, int blocksize, int cache, int order, const void *dx, void *dy,
+                   void *stream, float *seconds) {
+  return run_common(e, nblocks, blocksize, cache, order, dx, dy, stream, seconds, false);
+}
+
+wk_status wk_run_host(wk_engine *e, int mapped, int order, const void *x_host, void *y_host, void *stream) {
+  if (!e || !x_host || !y_host) return set_error(WK_ERR_INVALID, "NULL argument");
+  cudaStream_t st = S(stream);
+  const size_t xb = (size_t)e->ncols * dtype_size(e->dtype);
+  const size_t yb = (size_t)e->layout->info.nrows * (e->dtype == WK_F64 ? 8 : 4);
+  if (!e->xbuf.p) WK_TRY(e->xbuf.alloc(xb));
+  if (!e->ybuf.p) WK_TRY(e->ybuf.alloc(yb));
+  if (xb) WK_CUDA(cudaMemcpyAsync(e->xbuf.p, x_host, xb, cudaMemcpyHostToDevice, st));
+  if (e->layout->info.nznrows < e->layout->info.nrows) WK_CUDA(cudaMemsetAsync(e->ybuf.p, 0, yb, st));
+  RunArgs a{e, 0, 0, 1, order, mapped != 0, e->xbuf.p, e->ybuf.p, st};
+  WK_TRY(launch_spmv(a));
+  if (yb) WK_CUDA(cudaMemcpyAsync(y_host, e->ybuf.p, yb, cudaMemcpyDeviceToHost, st));
+  WK_CUDA(cudaStreamSynchronize(st));
+  return WK_OK;
+}
+
+wk_status wk_verify(const wk_layout *l, const double *orig, const double *comp, int *pass, int64_t *first_bad) {
+  if (!l || !orig || !comp || !pass) return set_error(WK_ERR_INVALID, "NULL argument");
+  const uint32_t n = l->info.nrows;
+  *pass = 1;
+  if (first_bad) *first_bad = -1;
+  for (uint32_t i = 0; i < n; i++) {
+    double o = orig[i], c = comp[i];
+    if ((std::fabs(o) <= 1e-14 && std::fabs(o - c) > 1e-14) ||
+        (std::fabs((o - c) / o) > 1e-5 && std::fabs(o) > 1e-14)) {
+      *pass = 0;
+      if (first_bad) *first_bad = i;
+      break;
+    }
+  }
+  return WK_OK;
+}
+
+wk_status wk_verify_x(const wk_layout *l, const double *orig, const double *comp, int strict, int *pass,
+                      int64_t *first_bad) {
+  if (!l || !orig || !comp || !pass) return set_error(WK_ERR_INVALID, "NULL argument");
+  const uint32_t n = l->info.nrows;
+  std::vector<int32_t> rm(n);
+  WK_TRY(wk_layout_get(l, WK_FIELD_ROW_MAP, rm.data(), n, nullptr));
+  *pass = 1;
+  if (first_bad) *first_bad = -1;
+  for (uint32_t i = 0; i < n; i++) {
+    double om = orig[rm[i]], c = comp[i];
+    double ou = strict ? om : orig[i];
+    if ((std::fabs(om) <= 1e-14 && std::fabs(ou - c) > 1e-14) ||
+        (std::fabs((om - c) / om) > 1e-5 && std::fabs(ou) > 1e-14)) {
+      *pass = 0;
+      if (first_bad) *first_bad = i;
+      break;
+    }
+  }
+  return WK_OK;
+}
+
+wk_status wk_fe_size(int dim, int ex, int ey, int ez, int dof, int64_t *nrows, int64_t *nnz) {
+  if (!nrows || !nnz) return set_error(WK_ERR_INVALID, "NULL argument");
+  if ((dim != 2 && dim != 3) || ex < 1 || ey < 1 || dof < 1 || (dim == 3 && ez < 1))
+    return set_error(WK_ERR_INVALID, "bad mesh");
+  int64_t nx = ex + 1, ny = ey + 1, nzn = dim == 3 ? ez + 1 : 1;
+  auto axis = [](int64_t n) { return n == 1 ? (int64_t)1 : 3 * n - 2; };  // sum of neighbour counts
+  *nrows = nx * ny * nzn * dof;
+  *nnz = axis(nx) * axis(ny) * axis(nzn) * dof * dof;
+  return WK_OK;
+}
+
+wk_status wk_fe_fill(int dim, int ex, int ey, int ez, int dof, int value_mode, uint64_t seed, int32_t *rowptr,
+                     int32_t *cols, double *vals, void *stream) {
+  int64_t n, z;
+  WK_TRY(wk_fe_size(dim, ex, ey, ez, dof, &n, &z));
+  if (z > 0x7fffffffLL) return set_error(WK_ERR_OVERFLOW, "nnz %lld exceeds INT32_MAX", (long long)z);
+  if (value_mode != 0 && value_mode != 1) return set_error(WK_ERR_INVALID, "value_mode %d", value_mode);
+  return launch_fe_fill(dim, ex, ey, ez, dof, value_mode, seed, rowptr, cols, vals, S(stream));
+}
+
+wk_status wk_uniform_vec(uint64_t seed, uint64_t stream_id, double *x, int64_t n, void *stream) {
+  if (!x || n < 0) return set_error(WK_ERR_INVALID, "bad argument");
+  return launch_uniform(seed, stream_id, x, n, S(stream));
+}
+
+wk_status wk_convert(const void *src, int sdt, void *dst, int ddt, int64_t n, void *stream) {
+  if (!src || !dst || n < 0 || !dtype_size(sdt) || !dtype_size(ddt))
+    return set_error(WK_ERR_INVALID, "bad argument");
+  return launch_convert(src, sdt, dst, ddt, n, S(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,161 @@
+// wk_internal.cuh -- shared definitions of libwarpkernel_gb300 (not installed).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+
+#include "../../include/wk_capi.h"
+
+namespace wk {
+
+// ---- errors ------------------------------------------------------------------
+wk_status set_error(wk_status code, const char *fmt, ...);
+const std::string &last_error();
+
+#define WK_CUDA(call)                                                              \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess)                                                         \
+      return ::wk::set_error(e_ == cudaErrorMemoryAllocation ? WK_ERR_ALLOC : WK_ERR_CUDA, \
+                             "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_),     \
+                             __FILE__, __LINE__);                                  \
+  } while (0)
+
+#define WK_TRY(call)                  \
+  do {                                \
+    wk_status s_ = (call);            \
+    if (s_ != WK_OK) return s_;       \
+  } while (0)
+
+#define WK_CHECK_LAUNCH() WK_CUDA(cudaGetLastError())
+
+// ---- device memory -------------------------------------------------------------
+// Owning device buffer (cudaMalloc / cudaFree).
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  DevBuf(DevBuf &&o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+  DevBuf &operator=(DevBuf &&o) noexcept {
+    if (this != &o) { release(); p = o.p; bytes = o.bytes; o.p = nullptr; o.bytes = 0; }
+    return *this;
+  }
+  ~DevBuf() { release(); }
+  wk_status alloc(size_t n) {
+    release();
+    if (n == 0) n = 16;  // keep a valid pointer for empty arrays
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      cudaGetLastError();
+      return set_error(e == cudaErrorMemoryAllocation ? WK_ERR_ALLOC : WK_ERR_CUDA,
+                       "cudaMalloc(%zu bytes) failed: %s", n, cudaGetErrorString(e));
+    }
+    bytes = n;
+    return WK_OK;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <class T>
+  T *as() const { return static_cast<T *>(p); }
+};
+
+// true if `ptr` is device (or managed) memory usable by kernels.
+bool is_device_ptr(const void *ptr);
+
+// A device view of a caller array: uses it in place if it is device memory,
+// otherwise uploads `bytes` into a temporary buffer on `stream`.
+struct DevView {
+  const void *dptr = nullptr;
+  DevBuf tmp;
+  wk_status from(const void *src, size_t bytes, cudaStream_t stream);
+};
+
+// Copies `bytes` from device `src` to caller memory `dst` (host or device).
+wk_status copy_out(void *dst, const void *src, size_t bytes, cudaStream_t stream);
+
+size_t dtype_size(int dtype);
+
+// ---- handles ---------------------------------------------------------------------
+struct LayoutDev {
+  // Reference fields (bit-identical to warpkernel.hpp's host scan).
+  int32_t *row_map = nullptr;          // [nrows]
+  int32_t *row_map_inv = nullptr;      // [nrows]
+  uint32_t *reorder_rows = nullptr;    // [nz]
+  int32_t *warp_offsets = nullptr;     // [nwarps+1]
+  uint32_t *max_nz_rows = nullptr;     // [nwarps]
+  uint32_t *threads_per_row = nullptr; // [nwarps]   (WPK2)
+  uint32_t *row_offset_warp = nullptr; // [nwarps+1] (WPK2)
+  // Working arrays of this implementation.
+  int32_t *rowptr = nullptr;           // [nrows+1] device copy of the CSR row offsets
+  uint32_t *slen = nullptr;            // [nrows]   row length in sorted order
+  int4 *warp_desc = nullptr;           // [nwarps]  {offset, steps, threads_per_row, first row}
+};
+
+}  // namespace wk
+
+struct wk_layout {
+  std::atomic<int> refs{1};
+  int device = 0;
+  wk_layout_info info{};
+  wk::LayoutDev d;
+  wk::DevBuf bufs[10];
+};
+
+struct wk_engine {
+  wk_layout *layout = nullptr;
+  int dtype = WK_F64;
+  uint32_t ncols = 0;
+  wk::DevBuf vals;   // allocate_nz values (padding 0)
+  wk::DevBuf cols;   // allocate_nz int32 column indices (padding 0)
+  wk::DevBuf status; // device status word for kernels that can report errors
+  wk::DevBuf xbuf, ybuf;  // staging vectors of wk_run_host (allocated on first use)
+};
+
+namespace wk {
+
+// ---- launchers (stream-ordered) ----------------------------------------------------
+// Builds all layout arrays from a device CSR row-pointer array (kind 1/2).
+wk_status build_layout(wk_layout *l, const int32_t *d_rowptr, int kind, int32_t threshold,
+                       cudaStream_t stream);
+// Padded gather of values (elem bytes 8/4/2) and column indices; cols are
+// optionally renumbered through row_map_inv.  Either output may be null.
+wk_status launch_process(const wk_layout *l, const void *vals, int elem_bytes,
+                         const int32_t *cols, void *pvals, int32_t *pcols, bool renumber,
+                         cudaStream_t stream);
+wk_status launch_reorder_columns(const wk_layout *l, const int32_t *cols, int32_t *out,
+                                 cudaStream_t stream);
+wk_status launch_reorder_x(const wk_layout *l, const void *x, void *xout, int elem_bytes,
+                           cudaStream_t stream);
+// Counts column indices outside [0, ncols) into *d_bad (device int).
+wk_status launch_check_cols(const int32_t *cols, size_t n, uint32_t ncols, int *d_bad,
+                            cudaStream_t stream);
+
+struct RunArgs {
+  const wk_engine *e;
+  int nblocks, blocksize, cache, order;
+  bool mapped;
+  const void *x;
+  void *y;
+  cudaStream_t stream;
+};
+wk_status launch_spmv(const RunArgs &a);
+
+wk_status launch_fe_fill(int dim, int ex, int ey, int ez, int dof, int value_mode, uint64_t seed,
+                         int32_t *rowptr, int32_t *cols, double *vals, cudaStream_t stream);
+wk_status launch_uniform(uint64_t seed, uint64_t stream_id, double *x, int64_t n,
+                         cudaStream_t stream);
+wk_status launch_convert(const void *src, int sdt, void *dst, int ddt, int64_t n,
+                         cudaStream_t stream);
+
+}  // namespace wk
