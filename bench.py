@@ -35,6 +35,14 @@ METRIC = "SpMV HBM GB/s (% of peak) and nnz/s, fp64 plain vs fp32/bf16 at stated
 WORKLOAD = dict(name="hex128_3dof_fp64_wpk2_run", dim=3, e=128, dof=3, value_mode=1, seed=1)
 
 
+def workload(args):
+    """The headline workload, or a smaller hex mesh of the same family (--mesh E)."""
+    W = dict(WORKLOAD)
+    if args.mesh != 128:
+        W.update(e=args.mesh, name=f"hex{args.mesh}_3dof_fp64_wpk2_run")
+    return W
+
+
 def alg_bytes(nrows, nnz, mapped=True):
     """fp64 run: 8 B value + 4 B column per nnz; per row 8 B x + 8 B y (+4 B row_map)."""
     return 12 * nnz + (20 if mapped else 16) * nrows
@@ -71,7 +79,7 @@ class Clocks:
     def __enter__(self):
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
                                       stdout=self.f, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.p = None
@@ -92,7 +100,7 @@ class Clocks:
         sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
         mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 5 + i and "Active" in r[5 + i]})
+        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 5 + i and r[5 + i].strip() == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(rows)}
 
@@ -146,7 +154,7 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    W = WORKLOAD
+    W = workload(args)
     rowptr, cols, vals = fe.fe_matrix(W["dim"], W["e"], W["e"], W["e"], W["dof"], W["value_mode"], W["seed"])
     n, nnz = rowptr.numel() - 1, cols.numel()
     x = fe.uniform_vec(W["seed"], 0, n)
@@ -210,12 +218,12 @@ def run_ours(args):
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(ms_per_step, 5),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded FE hex mesh generated on the device)",
-        "config": {"workload": W["name"], "mesh": "hex 128^3, 3 dof/node, random SPD element blocks",
+        "config": {"workload": W["name"], "mesh": f"hex {W['e']}^3, 3 dof/node, random SPD element blocks",
                    "nrows": n, "nnz": nnz, "layout": "WPK2" if args.kind == 2 else "WPK1",
                    "threshold": args.threshold if args.kind == 2 else None, "nwarps": k.nwarps,
                    "allocate_nz": k.allocate_nz, "order": "fast" if args.order == 0 else "exact",
                    "blocksize": bs, "nblocks": nb, "parallelism": f"replicas{world}",
-                   "l2": "inputs larger than L2 (6.3 GB matrix streamed per step), no flush"},
+                   "l2": f"inputs larger than L2 ({B / 1e9:.2f} GB streamed per step), no flush"},
         "nnz_per_s": round(world * nnz / (ms_per_step * 1e-3), 1),
         "gflops": round(world * 2 * nnz / (ms_per_step * 1e-3) / 1e9, 2),
         "pct_of_hbm_peak": round(100 * value / world / peak, 2),
@@ -253,7 +261,7 @@ def run_reference(args):
     world, rank, _ = dist_setup()
     if rank != 0:
         return None, rank
-    W = WORKLOAD
+    W = workload(args)
     rowptr, cols, vals = O.fe_matrix(W["dim"], W["e"], W["e"], W["e"], W["dof"], W["value_mode"], W["seed"])
     n, nnz = len(rowptr) - 1, len(cols)
     x = O.uniform_vec(W["seed"], 0, n)
@@ -293,13 +301,14 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--kind", type=int, default=2, choices=[1, 2])
     ap.add_argument("--threshold", type=int, default=81)
     ap.add_argument("--order", type=int, default=0, choices=[0, 1])
     ap.add_argument("--blocksize", type=int, default=256)
+    ap.add_argument("--mesh", type=int, default=128, help="hex elements per axis (128 = the headline)")
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
