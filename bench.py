@@ -307,7 +307,7 @@ def main():
     ap.add_argument("--kind", type=int, default=2, choices=[1, 2])
     ap.add_argument("--threshold", type=int, default=81)
     ap.add_argument("--order", type=int, default=0, choices=[0, 1])
-    ap.add_argument("--blocksize", type=int, default=256)
+    ap.add_argument("--blocksize", type=int, default=128)
     ap.add_argument("--mesh", type=int, default=128, help="hex elements per axis (128 = the headline)")
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -1,0 +1,394 @@
+/*
+ * warpkernel.hpp -- drop-in C++ surface of the GB300-native WPK SpMV.
+ *
+ * Replaces thejonwong/warpkernel's header of the same name (the reference's
+ * warpkernel.hpp:215-1022): classes warpkernel::structure, structure2,
+ * engine<ValueType, IndexType>, profiler and stats keep their names, member
+ * functions, argument meaning and public fields, so host code written
+ * against the reference (its wpk1.cu / wpk2.cu drivers) compiles with the
+ * container types swapped.  Everything runs through the C ABI of wk_capi.h:
+ * the layout is built on the GPU by hand-written sm_103a kernels and copied
+ * back into the public std::vector fields after each scan.
+ *
+ * Differences a user of the reference will notice:
+ *  - no CUSP: scan / reorder_* accept any container with size(), operator[]
+ *    (contiguous) and resize(); device vectors are warpkernel::device_array;
+ *  - errors throw warpkernel::error instead of asserting or exiting;
+ *  - run / run_x compute every row whatever the grid size (the reference's
+ *    2-D grid for nblocks > 65535 skipped rows, warpkernel.hpp:818-826) and
+ *    reject grids that do not cover all warps;
+ *  - the `cache` template flag selects L1-allocating x gathers (true) or
+ *    L2-only gathers (false); there are no texture references.
+ *
+ * Needs the CUDA runtime headers (cuda_runtime.h) and links against
+ * libwarpkernel_gb300.so and the CUDA runtime.
+ */
+#ifndef WARP_KERNEL_GB300_HPP
+#define WARP_KERNEL_GB300_HPP
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <iostream>
+#include <limits>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "wk_capi.h"
+
+#ifndef WARP_SIZE
+#define WARP_SIZE 32
+#endif
+
+namespace warpkernel {
+
+typedef unsigned int uint;
+
+class error : public std::runtime_error {
+ public:
+  error(wk_status s, const std::string &m) : std::runtime_error(m), status(s) {}
+  wk_status status;
+};
+
+inline void check(wk_status s) {
+  if (s != WK_OK) {
+    char buf[1024];
+    wk_last_error(buf, sizeof buf);
+    throw error(s, buf);
+  }
+}
+
+template <typename T>
+struct dtype_of;
+template <>
+struct dtype_of<double> {
+  static const int value = WK_F64;
+};
+template <>
+struct dtype_of<float> {
+  static const int value = WK_F32;
+};
+
+/* Owning device vector (stands in for cusp::array1d<T, device_memory>). */
+template <typename T>
+class device_array {
+ public:
+  device_array() {}
+  explicit device_array(size_t n, T v = T()) { assign(n, v); }
+  template <class Host, class = typename std::enable_if<!std::is_arithmetic<Host>::value>::type>
+  device_array(const Host &h) { *this = h; }
+  device_array(const device_array &o) { copy_from_device(o.p_, o.n_); }
+  ~device_array() { release(); }
+  device_array &operator=(const device_array &o) {
+    if (this != &o) copy_from_device(o.p_, o.n_);
+    return *this;
+  }
+  template <class Host, class = typename std::enable_if<!std::is_arithmetic<Host>::value>::type>
+  device_array &operator=(const Host &h) {
+    resize(h.size());
+    if (n_) check_cuda(cudaMemcpy(p_, &h[0], n_ * sizeof(T), cudaMemcpyHostToDevice));
+    return *this;
+  }
+  void resize(size_t n) {
+    if (n == n_) return;
+    release();
+    if (n) check_cuda(cudaMalloc(&p_, n * sizeof(T)));
+    n_ = n;
+  }
+  void assign(size_t n, T v) {
+    std::vector<T> h(n, v);
+    *this = h;
+  }
+  std::vector<T> to_host() const {
+    std::vector<T> h(n_);
+    if (n_) check_cuda(cudaMemcpy(h.data(), p_, n_ * sizeof(T), cudaMemcpyDeviceToHost));
+    return h;
+  }
+  operator std::vector<T>() const { return to_host(); }
+  T *data() { return p_; }
+  const T *data() const { return p_; }
+  size_t size() const { return n_; }
+
+ private:
+  static void check_cuda(cudaError_t e) {
+    if (e != cudaSuccess) throw error(WK_ERR_CUDA, cudaGetErrorString(e));
+  }
+  void copy_from_device(const T *src, size_t n) {
+    resize(n);
+    if (n) check_cuda(cudaMemcpy(p_, src, n * sizeof(T), cudaMemcpyDeviceToDevice));
+  }
+  void release() {
+    if (p_) cudaFree(p_);
+    p_ = nullptr;
+    n_ = 0;
+  }
+  T *p_ = nullptr;
+  size_t n_ = 0;
+};
+
+/* warpkernel::structure (reference warpkernel.hpp:215-551): WPK1 layout. */
+class structure {
+ public:
+  structure() {}
+  virtual ~structure() { release(); }
+  structure(const structure &) = delete;
+  structure &operator=(const structure &) = delete;
+
+  std::vector<int> row_map;      // y[row_map[i]] = y'[i]
+  std::vector<int> row_map_inv;  // new_colinds[n] = row_map_inv[colinds[n]]
+  std::vector<uint> reorder_rows;  // new_values[reorder_rows[i]] = A[i]
+  std::vector<int> reorder_A_rows;
+  std::vector<int> warp_offsets;
+  std::vector<uint> max_nz_rows;
+  uint nrows = 0, nznrows = 0, nz = 0, allocate_nz = 0, nwarps = 0;
+
+  /* structure::scan (warpkernel.hpp:309-365): only `rows` is read. */
+  template <typename ValueType, typename IndexType>
+  void scan(uint &nz_, uint &nrows_, ValueType *A, IndexType *rows, IndexType *colinds) {
+    static_assert(sizeof(IndexType) == 4, "32-bit row offsets expected");
+    (void)A;
+    (void)colinds;
+    release();
+    check(wk_scan1(reinterpret_cast<const int32_t *>(rows), nrows_, nz_, nullptr, &h_));
+    fetch();
+  }
+  /* scan of a CSR container with row_offsets / column_indices / values. */
+  template <class CSR>
+  void scan(uint &nz_, uint &nrows_, CSR &A) {
+    scan(nz_, nrows_, &A.values[0], &A.row_offsets[0], &A.column_indices[0]);
+  }
+
+  /* reorder_columns_coalesced (warpkernel.hpp:447-457): padded, renumbered. */
+  template <class Array>
+  void reorder_columns_coalesced(Array &colinds) {
+    std::vector<int32_t> out(allocate_nz);
+    check(wk_reorder_columns_coalesced(h_, reinterpret_cast<const int32_t *>(&colinds[0]), out.data(), nullptr));
+    colinds.resize(out.size());
+    for (size_t i = 0; i < out.size(); i++) colinds[i] = out[i];
+  }
+  /* reorder_columns (warpkernel.hpp:401-412): renumbered, CSR order. */
+  template <class Array>
+  void reorder_columns(Array &colinds) {
+    std::vector<int32_t> out(nz);
+    check(wk_reorder_columns(h_, reinterpret_cast<const int32_t *>(&colinds[0]), out.data(), nullptr));
+    for (size_t i = 0; i < out.size(); i++) colinds[i] = out[i];
+  }
+  /* reorder_x (warpkernel.hpp:518-530): device_x[row_map_inv[r]] = x[r]. */
+  template <class HostArray, typename T>
+  void reorder_x(HostArray &x, device_array<T> &device_x) {
+    device_x.resize(nrows);
+    check(wk_reorder_x(h_, dtype_of<T>::value, &x[0], device_x.data(), nullptr));
+  }
+
+  wk_layout *handle() const {
+    if (!h_) throw error(WK_ERR_STATE, "structure has not been scanned");
+    return h_;
+  }
+
+ protected:
+  void release() {
+    if (h_) wk_layout_destroy(h_);
+    h_ = nullptr;
+  }
+  template <typename T>
+  void get(int field, std::vector<T> &v) {
+    size_t n = 0;
+    check(wk_layout_get(h_, field, nullptr, 0, &n));
+    v.resize(n);
+    if (n) check(wk_layout_get(h_, field, v.data(), n, nullptr));
+  }
+  virtual void fetch() {
+    wk_layout_info i;
+    check(wk_layout_info_get(h_, &i));
+    nrows = i.nrows;
+    nznrows = i.nznrows;
+    nz = i.nz;
+    allocate_nz = i.allocate_nz;
+    nwarps = i.nwarps;
+    get(WK_FIELD_ROW_MAP, row_map);
+    get(WK_FIELD_ROW_MAP_INV, row_map_inv);
+    get(WK_FIELD_REORDER_ROWS, reorder_rows);
+    get(WK_FIELD_WARP_OFFSETS, warp_offsets);
+    get(WK_FIELD_MAX_NZ_ROWS, max_nz_rows);
+  }
+  wk_layout *h_ = nullptr;
+};
+
+/* warpkernel::structure2 (reference warpkernel.hpp:553-771): WPK2 layout. */
+class structure2 : public structure {
+ public:
+  std::vector<uint> row_offset_warp;
+  std::vector<uint> threads_per_row;
+  uint nmax_per_thread = 0;
+  uint min_nz = 0, max_nz = 0;
+
+  template <typename ValueType, typename IndexType>
+  void scan(uint &nz_, uint &nrows_, ValueType *A, IndexType *rows, IndexType *colinds, IndexType threshold) {
+    static_assert(sizeof(IndexType) == 4, "32-bit row offsets expected");
+    (void)A;
+    (void)colinds;
+    release();
+    check(wk_scan2(reinterpret_cast<const int32_t *>(rows), nrows_, nz_, (int32_t)threshold, nullptr, &h_));
+    fetch();
+  }
+  template <class CSR, typename IndexType>
+  void scan(uint &nz_, uint &nrows_, CSR &A, IndexType threshold) {
+    scan(nz_, nrows_, &A.values[0], &A.row_offsets[0], &A.column_indices[0], threshold);
+  }
+
+ protected:
+  void fetch() override {
+    structure::fetch();
+    wk_layout_info i;
+    check(wk_layout_info_get(h_, &i));
+    nmax_per_thread = i.nmax_per_thread;
+    min_nz = i.min_nz;
+    max_nz = i.max_nz;
+    get(WK_FIELD_ROW_OFFSET_WARP, row_offset_warp);
+    get(WK_FIELD_THREADS_PER_ROW, threads_per_row);
+  }
+};
+
+/* warpkernel::engine (reference warpkernel.hpp:773-959). */
+template <typename ValueType, typename IndexType>
+class engine {
+  static_assert(sizeof(IndexType) == 4, "32-bit column indices expected");
+
+ public:
+  /* engine.device_colinds: assignable from a host array of allocate_nz
+   * padded column indices (wpk1.cu:175, 198), readable as a host vector. */
+  class colinds_proxy {
+   public:
+    explicit colinds_proxy(engine *e) : e_(e) {}
+    template <class Array>
+    colinds_proxy &operator=(const Array &a) {
+      check(wk_engine_set_colinds(e_->handle(), reinterpret_cast<const int32_t *>(&a[0]), nullptr));
+      return *this;
+    }
+    colinds_proxy &operator=(const colinds_proxy &o) { return *this = o.to_host(); }
+    std::vector<IndexType> to_host() const {
+      std::vector<IndexType> v(e_->kernel->allocate_nz);
+      check(wk_engine_get_colinds(e_->handle(), reinterpret_cast<int32_t *>(v.data()), v.size()));
+      return v;
+    }
+    operator std::vector<IndexType>() const { return to_host(); }
+
+   private:
+    engine *e_;
+  };
+  colinds_proxy device_colinds{this};
+
+  explicit engine(structure &k) : kernel(&k) {}
+  engine(structure &k, ValueType *A, IndexType *colinds) : kernel(&k) { create(A, colinds); }
+  engine(structure2 &k, ValueType *A, IndexType *colinds) : kernel(&k) { create(A, colinds); }
+  ~engine() {
+    if (h_) wk_engine_destroy(h_);
+  }
+  engine(const engine &) = delete;
+  engine &operator=(const engine &) = delete;
+
+  /* run<cache>(nblocks, blocksize, dx, dy): y[row_map[p]] = row sums; returns
+   * the kernel time in seconds (synchronous, like the reference). */
+  template <bool cache>
+  float run(int nblocks, int blocksize, ValueType *dx, ValueType *dy) {
+    float s = 0.f;
+    check(wk_run(handle(), nblocks, blocksize, cache ? 1 : 0, order, dx, dy, nullptr, &s));
+    return s;
+  }
+  /* run_x<cache>(...): y'[p] = sorted-row sums with the reordered x. */
+  template <bool cache>
+  float run_x(int nblocks, int blocksize, ValueType *dx, ValueType *dy) {
+    float s = 0.f;
+    check(wk_run_x(handle(), nblocks, blocksize, cache ? 1 : 0, order, dx, dy, nullptr, &s));
+    return s;
+  }
+
+  /* verify (warpkernel.hpp:932-943). */
+  template <typename R>
+  bool verify(R orig, R comp) {
+    std::vector<double> o(kernel->nrows), c(kernel->nrows);
+    for (uint i = 0; i < kernel->nrows; i++) {
+      o[i] = (double)orig[i];
+      c[i] = (double)comp[i];
+    }
+    int pass = 0;
+    int64_t bad = -1;
+    check(wk_verify(kernel->handle(), o.data(), c.data(), &pass, &bad));
+    if (!pass)
+      std::cout << "verify: " << o[bad] << "\t" << c[bad] << "\t" << bad << " "
+                << std::fabs((o[bad] - c[bad]) / o[bad]) << std::endl;
+    return pass != 0;
+  }
+  /* verify_x (warpkernel.hpp:945-957), with the reference's condition. */
+  template <typename R>
+  bool verify_x(R orig, R comp) {
+    std::vector<double> o(kernel->nrows), c(kernel->nrows);
+    for (uint i = 0; i < kernel->nrows; i++) {
+      o[i] = (double)orig[i];
+      c[i] = (double)comp[i];
+    }
+    int pass = 0;
+    int64_t bad = -1;
+    check(wk_verify_x(kernel->handle(), o.data(), c.data(), 0, &pass, &bad));
+    if (!pass) std::cout << "verify_x: " << o[kernel->row_map[bad]] << "\t" << c[bad] << "\t" << bad << std::endl;
+    return pass != 0;
+  }
+
+  wk_engine *handle() const {
+    if (!h_) throw error(WK_ERR_STATE, "engine was constructed without values");
+    return h_;
+  }
+
+  /* WK_ORDER_FAST (default) or WK_ORDER_EXACT (the reference's order). */
+  int order = WK_ORDER_FAST;
+  structure *kernel;
+
+ private:
+  void create(ValueType *A, IndexType *colinds) {
+    check(wk_engine_create(kernel->handle(), dtype_of<ValueType>::value, A,
+                           reinterpret_cast<const int32_t *>(colinds), kernel->nrows, nullptr, &h_));
+  }
+  wk_engine *h_ = nullptr;
+};
+
+/* profiler (warpkernel.hpp:963-982). */
+class profiler {
+ public:
+  double sum = 0.0;
+  int count = 0;
+  void add(double secs) {
+    sum += secs;
+    count++;
+  }
+  double avg() { return sum / (1. * count); }
+};
+
+/* stats (warpkernel.hpp:984-1022). */
+class stats {
+ public:
+  stats() : min_(std::numeric_limits<double>::max()), max_(0.) {}
+  void add(double val, std::string ident = "") {
+    if (val < min_) {
+      min_ = val;
+      min_str_ = ident;
+    }
+    if (val > max_) {
+      max_ = val;
+      max_str_ = ident;
+    }
+  }
+  double Min() { return min_; }
+  std::string Min_str() { return min_str_; }
+  double Max() { return max_; }
+  std::string Max_str() { return max_str_; }
+
+ protected:
+  double min_, max_;
+  std::string min_str_, max_str_;
+};
+
+}  // namespace warpkernel
+
+#endif

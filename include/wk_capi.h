@@ -185,6 +185,18 @@ wk_status wk_run_x(wk_engine *e, int nblocks, int blocksize, int cache, int orde
 wk_status wk_run_host(wk_engine *e, int mapped, int order, const void *x_host, void *y_host,
                       void *stream);
 
+/* ---- solver building blocks (no reference counterpart) ------------------ */
+
+/* Residual of an fp64 engine: r = b - A x for every row (rows without
+ * entries get r = b) and, if norm2 is non-NULL, *norm2 = ||r||^2 written to
+ * DEVICE memory.  x (ncols), b, r (nrows) and norm2 are device pointers.  The
+ * norm is reduced in a fixed order (bit-reproducible).  Uses an engine-owned
+ * device buffer of per-block partial sums, allocated on the first call.
+ * The residual of the iterative-refinement solve, which the spec asks
+ * to keep in fp64. */
+wk_status wk_residual(wk_engine *e, const double *x, const double *b, double *r, double *norm2,
+                      void *stream);
+
 /* ---- verification ------------------------------------------------------- */
 
 /* engine::verify(orig, comp) -- warpkernel.hpp:932-943 (host arrays of nrows

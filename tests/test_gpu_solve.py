@@ -1,0 +1,60 @@
+"""Solver building blocks on the GPU: the fp64 residual r = b - A x and its
+norm, against the oracle."""
+import numpy as np
+import pytest
+
+from conftest import random_csr
+from oracle import wk_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-12
+
+
+def setup(rp, cols, vals, kind=1, th=0):
+    import warpkernel_gb300 as wk
+    k = wk.structure() if kind == 1 else wk.structure2()
+    k.scan(len(cols), len(rp) - 1, None, rp, None, *(() if kind == 1 else (th,)))
+    return k, wk.engine(k, vals, cols)
+
+
+def test_residual_matches_oracle():
+    import torch
+    cases = [O.fe_matrix(3, 10, 10, 10, 3, value_mode=1, seed=4), O.fe_matrix(2, 64, 64, 0, 1, value_mode=0)]
+    rng = np.random.default_rng(8)
+    cases.append(random_csr(rng, 3000, 40, p_empty=0.3))
+    for rp, cols, vals in cases:
+        n = len(rp) - 1
+        for kind, th in ((1, 0), (2, 7)):
+            k, eng = setup(rp, cols, vals, kind, th)
+            x = rng.uniform(-1, 1, n)
+            b = rng.uniform(-1, 1, n)
+            y = O.csr_spmv(rp, cols, vals, x)
+            r_ref = b - y
+            dx, db = torch.from_numpy(x).cuda(), torch.from_numpy(b).cuda()
+            r = torch.full((n,), np.nan, dtype=torch.float64, device="cuda")
+            nrm = torch.zeros(1, dtype=torch.float64, device="cuda")
+            eng.residual(dx, db, r, nrm)
+            rh = r.cpu().numpy()
+            assert np.linalg.norm(rh - r_ref) / np.linalg.norm(r_ref) < REL_TOL
+            empty = np.diff(rp) == 0
+            assert np.array_equal(rh[empty], b[empty])
+            ref2 = float(np.dot(r_ref, r_ref))
+            assert abs(nrm.item() - ref2) / ref2 < REL_TOL
+            # deterministic: a second call gives identical bits
+            r2 = torch.empty_like(r)
+            nrm2 = torch.zeros(1, dtype=torch.float64, device="cuda")
+            eng.residual(dx, db, r2, nrm2)
+            assert torch.equal(r, r2) and nrm.item() == nrm2.item()
+
+
+def test_residual_rejects_low_precision_engine():
+    import torch
+
+    import warpkernel_gb300 as wk
+    rp, cols, vals = O.fe_matrix(2, 8, 8, 0, 1, value_mode=0)
+    k = wk.structure().scan(len(cols), len(rp) - 1, None, rp)
+    eng = wk.engine(k, vals.astype(np.float32), cols, dtype="f32")
+    t = torch.zeros(len(rp) - 1, dtype=torch.float64, device="cuda")
+    with pytest.raises(wk.WKError, match="F64"):
+        eng.residual(t, t, t)

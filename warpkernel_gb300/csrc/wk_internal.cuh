@@ -120,6 +120,7 @@ struct wk_engine {
   wk::DevBuf cols;   // allocate_nz int32 column indices (padding 0)
   wk::DevBuf status; // device status word for kernels that can report errors
   wk::DevBuf xbuf, ybuf;  // staging vectors of wk_run_host (allocated on first use)
+  wk::DevBuf scratch;     // per-block partial sums of the solver kernels (grown on demand)
 };
 
 namespace wk {
@@ -150,6 +151,8 @@ struct RunArgs {
   cudaStream_t stream;
 };
 wk_status launch_spmv(const RunArgs &a);
+// Grid / block of a one-warp-per-layout-warp launch (nblocks/blocksize <= 0: automatic).
+wk_status launch_shape(uint32_t W, int nblocks, int blocksize, unsigned *grid, unsigned *block);
 
 wk_status launch_fe_fill(int dim, int ex, int ey, int ez, int dof, int value_mode, uint64_t seed,
                          int32_t *rowptr, int32_t *cols, double *vals, cudaStream_t stream);

@@ -1,0 +1,192 @@
+// wk_spmv_core.cuh -- device building blocks shared by the SpMV kernels and
+// the solver kernels: streaming loads with L2 eviction hints, x gathers, and
+// the per-warp row sums of a WPK1/WPK2 layout warp.
+//
+// Layout: layout warp w owns slots [o_w, o_w + 32*A_w); entry i of layout lane
+// l sits at o_w + l + 32*i (warpkernel.hpp:65-71, 360-361).  Layout lane l
+// belongs to sorted row first_row_w + l / T_w; the T_w lanes of a row are
+// summed by a tree (T_w = 1 for WPK1).
+#pragma once
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+namespace wk {
+namespace core {
+
+constexpr int WS = 32;
+
+__device__ __forceinline__ uint64_t policy_evict_first() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+
+// ---- streaming loads (matrix), ld.global.nc.L1::no_allocate + evict_first ------
+__device__ __forceinline__ void ld_stream(const double *p, double (&v)[4], uint64_t pol) {
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f64 {%0,%1,%2,%3}, [%4], %5;"
+               : "=d"(v[0]), "=d"(v[1]), "=d"(v[2]), "=d"(v[3])
+               : "l"(p), "l"(pol));
+}
+__device__ __forceinline__ void ld_stream(const float *p, float (&v)[4], uint64_t pol) {
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f32 {%0,%1,%2,%3}, [%4], %5;"
+               : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3])
+               : "l"(p), "l"(pol));
+}
+__device__ __forceinline__ void ld_stream(const __nv_bfloat16 *p, __nv_bfloat16 (&v)[4], uint64_t pol) {
+  unsigned a, b;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.b32 {%0,%1}, [%2], %3;"
+               : "=r"(a), "=r"(b)
+               : "l"(p), "l"(pol));
+  v[0] = __ushort_as_bfloat16((unsigned short)(a & 0xffffu));
+  v[1] = __ushort_as_bfloat16((unsigned short)(a >> 16));
+  v[2] = __ushort_as_bfloat16((unsigned short)(b & 0xffffu));
+  v[3] = __ushort_as_bfloat16((unsigned short)(b >> 16));
+}
+__device__ __forceinline__ void ld_stream4(const int32_t *p, int (&c)[4], uint64_t pol) {
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.s32 {%0,%1,%2,%3}, [%4], %5;"
+               : "=r"(c[0]), "=r"(c[1]), "=r"(c[2]), "=r"(c[3])
+               : "l"(p), "l"(pol));
+}
+template <typename T>
+__device__ __forceinline__ T ld_stream1(const T *p, uint64_t pol);
+template <>
+__device__ __forceinline__ double ld_stream1(const double *p, uint64_t pol) {
+  double v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
+  return v;
+}
+template <>
+__device__ __forceinline__ float ld_stream1(const float *p, uint64_t pol) {
+  float v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+  return v;
+}
+template <>
+__device__ __forceinline__ int32_t ld_stream1(const int32_t *p, uint64_t pol) {
+  int v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+  return v;
+}
+template <>
+__device__ __forceinline__ __nv_bfloat16 ld_stream1(const __nv_bfloat16 *p, uint64_t pol) {
+  unsigned short v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(v) : "l"(p), "l"(pol));
+  return __ushort_as_bfloat16(v);
+}
+
+// ---- type traits: value/vector element -> accumulator ------------------------------
+template <typename V>
+struct Tr;
+template <>
+struct Tr<double> {
+  typedef double Acc;
+  static __device__ __forceinline__ double acc(double v) { return v; }
+};
+template <>
+struct Tr<float> {
+  typedef float Acc;
+  static __device__ __forceinline__ float acc(float v) { return v; }
+};
+template <>
+struct Tr<__nv_bfloat16> {
+  typedef float Acc;
+  static __device__ __forceinline__ float acc(__nv_bfloat16 v) { return __bfloat162float(v); }
+};
+
+// ---- gathers (x): L1-allocating (`cache`, the texture path of the reference) or L2 only
+template <bool L1>
+__device__ __forceinline__ double gather(const double *x, int i) { return L1 ? __ldg(x + i) : __ldcg(x + i); }
+template <bool L1>
+__device__ __forceinline__ float gather(const float *x, int i) { return L1 ? __ldg(x + i) : __ldcg(x + i); }
+template <bool L1>
+__device__ __forceinline__ __nv_bfloat16 gather(const __nv_bfloat16 *x, int i) {
+  const unsigned short *u = reinterpret_cast<const unsigned short *>(x);
+  return __ushort_as_bfloat16(L1 ? __ldg(u + i) : __ldcg(u + i));
+}
+
+__device__ __forceinline__ double fma_acc(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fma_acc(float a, float b, float c) { return fmaf(a, b, c); }
+
+// Tree over the T lanes of a row: lockstep semantics of warpkernel.hpp:157-162,
+// i.e. s_l <- s_l + s_{l+k} for k = 1, 2, 4, ... (all reads before writes).
+template <typename Acc>
+__device__ __forceinline__ Acc row_tree(Acc s, uint32_t T) {
+  for (uint32_t k = 1; k < T; k <<= 1) s += __shfl_down_sync(0xffffffffu, s, k);
+  return s;
+}
+
+// Exact order: layout lane `lane` sums its slots first product, then fma per
+// step (warpkernel.hpp:147-153).  Returns 0 for lanes of absent rows.
+template <typename V, typename X, bool L1>
+__device__ __forceinline__ typename Tr<V>::Acc lane_sum_exact(const V *__restrict__ pv,
+                                                             const int32_t *__restrict__ pc, int4 d,
+                                                             const X *__restrict__ x, uint32_t lane,
+                                                             bool valid) {
+  typedef typename Tr<V>::Acc Acc;
+  Acc s = Acc(0);
+  if (valid) {
+    size_t o = (size_t)(uint32_t)d.x + lane;
+    const size_t end = o + (size_t)WS * (uint32_t)d.y;
+    s = Tr<V>::acc(pv[o]) * (Acc)Tr<X>::acc(gather<L1>(x, pc[o]));
+    for (o += WS; o < end; o += WS) s = fma_acc(Tr<V>::acc(pv[o]), (Acc)Tr<X>::acc(gather<L1>(x, pc[o])), s);
+  }
+  return s;
+}
+
+// Fast order: each lane streams 4 consecutive slots of a 4-step unit (slots
+// 4j..4j+3 = layout lanes 4(j%8)..4(j%8)+3 at step j/8) with one 256-bit
+// (fp64), 128-bit (fp32) or 64-bit (bf16) value load and one 128-bit column
+// load; partials are combined across the four lanes holding the same layout
+// lanes (xor 8, xor 16) and moved to the owning lane; the A_w % 4 remaining
+// steps are added one slot per lane.  Returns layout lane `lane`'s total.
+template <typename V, typename X, bool L1>
+__device__ __forceinline__ typename Tr<V>::Acc lane_sum_fast(const V *__restrict__ pv,
+                                                            const int32_t *__restrict__ pc, int4 d,
+                                                            const X *__restrict__ x, uint32_t lane,
+                                                            uint64_t pol) {
+  typedef typename Tr<V>::Acc Acc;
+  const uint32_t A = (uint32_t)d.y;
+  const size_t o = (size_t)(uint32_t)d.x;
+  const uint32_t units = A >> 2, rem = A & 3u;
+  Acc a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+  const V *vp = pv + o + 4 * lane;
+  const int32_t *cp = pc + o + 4 * lane;
+#pragma unroll 2
+  for (uint32_t u = 0; u < units; u++) {
+    V v[4];
+    int c[4];
+    ld_stream(vp, v, pol);
+    ld_stream4(cp, c, pol);
+    a0 = fma_acc(Tr<V>::acc(v[0]), (Acc)Tr<X>::acc(gather<L1>(x, c[0])), a0);
+    a1 = fma_acc(Tr<V>::acc(v[1]), (Acc)Tr<X>::acc(gather<L1>(x, c[1])), a1);
+    a2 = fma_acc(Tr<V>::acc(v[2]), (Acc)Tr<X>::acc(gather<L1>(x, c[2])), a2);
+    a3 = fma_acc(Tr<V>::acc(v[3]), (Acc)Tr<X>::acc(gather<L1>(x, c[3])), a3);
+    vp += 4 * WS;
+    cp += 4 * WS;
+  }
+  // remaining steps, one slot per lane (issued before the shuffles)
+  Acc tail = Acc(0);
+  size_t ot = o + (size_t)units * 4 * WS + lane;
+  for (uint32_t i = 0; i < rem; i++, ot += WS)
+    tail = fma_acc(Tr<V>::acc(ld_stream1(pv + ot, pol)), (Acc)Tr<X>::acc(gather<L1>(x, ld_stream1(pc + ot, pol))),
+                   tail);
+  a0 += __shfl_xor_sync(0xffffffffu, a0, 8);
+  a1 += __shfl_xor_sync(0xffffffffu, a1, 8);
+  a2 += __shfl_xor_sync(0xffffffffu, a2, 8);
+  a3 += __shfl_xor_sync(0xffffffffu, a3, 8);
+  a0 += __shfl_xor_sync(0xffffffffu, a0, 16);
+  a1 += __shfl_xor_sync(0xffffffffu, a1, 16);
+  a2 += __shfl_xor_sync(0xffffffffu, a2, 16);
+  a3 += __shfl_xor_sync(0xffffffffu, a3, 16);
+  const int src = (int)(lane >> 2);
+  Acc t0 = __shfl_sync(0xffffffffu, a0, src);
+  Acc t1 = __shfl_sync(0xffffffffu, a1, src);
+  Acc t2 = __shfl_sync(0xffffffffu, a2, src);
+  Acc t3 = __shfl_sync(0xffffffffu, a3, src);
+  const uint32_t k = lane & 3u;
+  Acc s = k == 0 ? t0 : k == 1 ? t1 : k == 2 ? t2 : t3;
+  return s + tail;
+}
+
+}  // namespace core
+}  // namespace wk

@@ -284,6 +284,12 @@ class engine:
                                  _stream_ptr(stream)))
         return y_host
 
+    def residual(self, x, b, r, norm2=None, stream=None):
+        """r = b - A x (fp64 engine, device tensors); norm2: optional 1-element
+        float64 CUDA tensor receiving ||r||^2."""
+        check(load().wk_residual(self.handle, _ptr(x), _ptr(b), _ptr(r), _ptr(norm2), _stream_ptr(stream)))
+        return r
+
     def verify(self, orig, comp):
         """engine::verify (warpkernel.hpp:932-943) on host arrays."""
         o = np.ascontiguousarray(orig, np.float64)
