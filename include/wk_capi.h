@@ -197,6 +197,23 @@ wk_status wk_run_host(wk_engine *e, int mapped, int order, const void *x_host, v
 wk_status wk_residual(wk_engine *e, const double *x, const double *b, double *r, double *norm2,
                       void *stream);
 
+/* wk_residual without any device allocation.  No counterpart in the
+ * reference.  For callers that must not call cudaMalloc while they run --
+ * e.g. a solver plugin inside a host application that owns the GPU's whole
+ * memory budget, or a latency-critical loop that cannot afford cudaMalloc's
+ * implicit device synchronisation.  Same inputs, outputs and results as
+ * wk_residual (the caller still provides x, b, r and norm2); the per-block
+ * partial sums go to a static device array of 65,536 doubles (512 KiB) that
+ * every GPU loading the library keeps until the process exits.  Layouts with
+ * more than 262,144 warps are rejected with WK_ERR_INVALID.  The first call on
+ * a device looks up that array's address (cudaGetSymbolAddress), so make it
+ * once per device before any stream capture.  All calls share the array:
+ * calls whose kernels overlap on the GPU (other streams, other threads) race
+ * and must be serialised by the caller.  Creating the engine allocates; this
+ * call does not. */
+wk_status wk_residual_static(wk_engine *e, const double *x, const double *b, double *r, double *norm2,
+                             void *stream);
+
 /* ---- verification ------------------------------------------------------- */
 
 /* engine::verify(orig, comp) -- warpkernel.hpp:932-943 (host arrays of nrows

@@ -59,6 +59,7 @@ SIGNATURES = {
     "wk_run_x": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, _fp]),
     "wk_run_host": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, vp]),
     "wk_residual": (C.c_int, [vp, vp, vp, vp, vp, vp]),
+    "wk_residual_static": (C.c_int, [vp, vp, vp, vp, vp, vp]),
     "wk_verify": (C.c_int, [vp, vp, vp, _ip, _i64p]),
     "wk_verify_x": (C.c_int, [vp, vp, vp, C.c_int, _ip, _i64p]),
     "wk_fe_size": (C.c_int, [C.c_int] * 5 + [_i64p, _i64p]),

@@ -101,7 +101,56 @@ wk_status launch_residual(const wk_engine *e, const double *x, const double *b, 
 
 }  // namespace wk
 
+// ---- residual without any device allocation -------------------------------------
+// The partial sums of wk_residual_static live in this fixed array instead of
+// an engine-owned buffer.  Every GPU that loads the library holds it (512 KiB)
+// until the process exits.  All calls share it: each call first writes
+// partials[0, grid) and only then sums them, so no contents need clearing,
+// but calls whose kernels overlap on the GPU race on it.
+namespace wk {
+namespace {
+constexpr unsigned kResidualStaticBlocks = 65536;  // one double per block
+static __device__ __align__(256) double g_residual_partials[kResidualStaticBlocks];
+
+constexpr int kMaxDevices = 64;
+std::atomic<double *> g_residual_partials_addr[kMaxDevices];
+
+// Device address of g_residual_partials on the current device, looked up on
+// the first call per device (cudaGetSymbolAddress with that device current).
+wk_status static_partials(double **out) {
+  int dev = 0;
+  WK_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return set_error(WK_ERR_STATE, "device %d beyond the supported %d", dev, kMaxDevices);
+  double *p = g_residual_partials_addr[dev].load();
+  if (!p) {
+    cudaError_t e = cudaGetSymbolAddress((void **)&p, g_residual_partials);
+    if (e != cudaSuccess || !p)
+      return set_error(WK_ERR_CUDA, "cudaGetSymbolAddress(g_residual_partials) on device %d failed: %s", dev,
+                       cudaGetErrorString(e));
+    g_residual_partials_addr[dev].store(p);
+  }
+  *out = p;
+  return WK_OK;
+}
+}  // namespace
+}  // namespace wk
+
 using namespace wk;
+
+extern "C" wk_status wk_residual_static(wk_engine *e, const double *x, const double *b, double *r,
+                                        double *norm2, void *stream) {
+  if (!e || !x || !b || !r) return set_error(WK_ERR_INVALID, "NULL argument");
+  if (e->dtype != WK_F64) return set_error(WK_ERR_INVALID, "wk_residual_static needs a WK_F64 engine");
+  const unsigned grid = residual_grid(e->layout);
+  if (grid > kResidualStaticBlocks)
+    return set_error(WK_ERR_INVALID,
+                     "wk_residual_static: the layout has %u warps and needs %u partial sums, but the static "
+                     "scratch holds %u (at most %u layout warps); use wk_residual",
+                     e->layout->info.nwarps, grid, kResidualStaticBlocks, kResidualStaticBlocks * (128u / 32u));
+  double *partials = nullptr;
+  WK_TRY(static_partials(&partials));
+  return launch_residual(e, x, b, r, partials, grid, norm2, (cudaStream_t)stream);
+}
 
 extern "C" wk_status wk_residual(wk_engine *e, const double *x, const double *b, double *r, double *norm2,
                                  void *stream) {
