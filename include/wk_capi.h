@@ -148,6 +148,15 @@ wk_status wk_engine_get_colinds(const wk_engine *e, int32_t *dst, size_t cap);
 
 wk_status wk_engine_destroy(wk_engine *e);
 
+/* Adds a compact column storage to the engine (no reference counterpart;
+ * the mixed-precision paths): every layout warp whose real entries span fewer
+ * than 65,536 columns stores them as 16-bit offsets from a per-warp base, the
+ * others keep 32-bit indices in a side array.  Afterwards WK_ORDER_FAST runs
+ * stream 2 B instead of 4 B of index per slot; results are bit-identical to
+ * the uncompressed fast order.  *wide_warps (optional) = warps left 32-bit.
+ * wk_engine_set_colinds rebuilds the compact storage. */
+wk_status wk_engine_compress_cols(wk_engine *e, void *stream, uint32_t *wide_warps);
+
 /* ---- SpMV --------------------------------------------------------------- */
 
 /* Accumulation order of wk_run / wk_run_x. */
@@ -213,6 +222,40 @@ wk_status wk_residual(wk_engine *e, const double *x, const double *b, double *r,
  * call does not. */
 wk_status wk_residual_static(wk_engine *e, const double *x, const double *b, double *r, double *norm2,
                              void *stream);
+
+/* Conjugate-gradient solves of A x = b for a symmetric positive definite A
+ * (no reference counterpart; the north-star's refined solve).  Inputs: tol
+ * (target ||b - A x|| / ||b||), max_iter (CG iterations, or outer refinement
+ * steps for wk_ir_cg), max_inner / inner_tol (inner CG iterations and the
+ * relative reduction each inner solve aims for), check_every (iterations
+ * between host-side convergence checks; scalars otherwise stay on the
+ * device).  Outputs: iters (CG iterations; for wk_ir_cg the inner total),
+ * outer, relres (the fp64 relative residual of the returned x) and seconds
+ * (device time of the whole solve, CUDA events).  Returns WK_ERR_NOTCONV if
+ * tol was not reached. */
+typedef struct {
+  double tol;
+  int max_iter;
+  int max_inner;
+  double inner_tol;
+  int check_every;
+  int iters;
+  int outer;
+  double relres;
+  double seconds;
+} wk_cg_params;
+
+/* fp64 CG on an fp64 engine; b, x (initial guess, overwritten) are device
+ * vectors of nrows doubles. */
+wk_status wk_cg(wk_engine *e, const double *b, double *x, wk_cg_params *p, void *stream);
+
+/* Iterative-refinement CG: the residual b - A x, its norm, the dot products of
+ * the outer loop and the update x += d stay fp64 (engine e64); each
+ * correction d solves A d = r with an fp32 CG on the low-precision engine `lo`
+ * (WK_F32 or WK_BF16 values, fp32 vectors, compressed columns if
+ * wk_engine_compress_cols was called). */
+wk_status wk_ir_cg(wk_engine *e64, wk_engine *lo, const double *b, double *x, wk_cg_params *p,
+                   void *stream);
 
 /* ---- verification ------------------------------------------------------- */
 

@@ -58,3 +58,64 @@ def test_residual_rejects_low_precision_engine():
     t = torch.zeros(len(rp) - 1, dtype=torch.float64, device="cuda")
     with pytest.raises(wk.WKError, match="F64"):
         eng.residual(t, t, t)
+
+
+def _spd_case(e=8, seed=4):
+    rp, cols, vals = O.fe_matrix(3, e, e, e, 3, value_mode=1, seed=seed)
+    n = len(rp) - 1
+    A = np.zeros((n, n))
+    for r in range(n):
+        A[r, cols[rp[r]:rp[r + 1]]] = vals[rp[r]:rp[r + 1]]
+    return rp, cols, vals, A
+
+
+def test_cg_fp64_converges_to_the_dense_solution():
+    import torch
+
+    import warpkernel_gb300 as wk
+    rp, cols, vals, A = _spd_case()
+    n = len(rp) - 1
+    xs = O.uniform_vec(2, 0, n)
+    b = A @ xs
+    for kind, th in ((1, 0), (2, 27)):
+        k, eng = setup(rp, cols, vals, kind, th)
+        db = torch.from_numpy(b).cuda()
+        x = torch.zeros(n, dtype=torch.float64, device="cuda")
+        res = wk.wpk.cg(eng, db, x, tol=1e-10)
+        assert res["converged"] and res["relres"] <= 1e-10, res
+        xh = x.cpu().numpy()
+        assert np.linalg.norm(b - A @ xh) / np.linalg.norm(b) <= 1.1e-10
+        assert np.linalg.norm(xh - xs) / np.linalg.norm(xs) < 1e-6  # A is well enough conditioned here
+
+
+def test_ir_cg_reaches_fp64_tolerance_with_fp32_and_bf16_inner():
+    import torch
+
+    import warpkernel_gb300 as wk
+    rp, cols, vals, A = _spd_case(seed=9)
+    n = len(rp) - 1
+    b = A @ O.uniform_vec(3, 0, n)
+    db = torch.from_numpy(b).cuda()
+    k, e64 = setup(rp, cols, vals, 2, 27)
+    for dtype, tdt in (("f32", torch.float32), ("bf16", torch.bfloat16)):
+        lo = wk.engine(k, wk.fe.convert(torch.from_numpy(vals).cuda(), tdt), torch.from_numpy(cols).cuda(),
+                       dtype=dtype)
+        lo.compress_cols()
+        x = torch.zeros(n, dtype=torch.float64, device="cuda")
+        res = wk.wpk.ir_cg(e64, lo, db, x, tol=1e-10, inner_tol=1e-3 if dtype == "bf16" else 1e-4)
+        assert res["converged"] and res["relres"] <= 1e-10 and res["outer"] >= 2, (dtype, res)
+        xh = x.cpu().numpy()
+        assert np.linalg.norm(b - A @ xh) / np.linalg.norm(b) <= 1.1e-10
+
+
+def test_cg_reports_non_convergence():
+    import torch
+
+    import warpkernel_gb300 as wk
+    rp, cols, vals, A = _spd_case()
+    n = len(rp) - 1
+    k, eng = setup(rp, cols, vals)
+    b = torch.from_numpy(A @ np.ones(n)).cuda()
+    x = torch.zeros(n, dtype=torch.float64, device="cuda")
+    res = wk.wpk.cg(eng, b, x, tol=1e-14, max_iter=3, check_every=1)
+    assert not res["converged"] and res["iters"] == 3 and res["relres"] > 1e-14

@@ -199,3 +199,38 @@ def test_device_generator_matches_cpu_generator():
     x = O.uniform_vec(3, 1, 1000)
     assert np.array_equal(bits(wk().fe.uniform_vec(3, 1, 1000).cpu().numpy()), bits(x))
     assert t.cuda.is_available()
+
+
+def test_compressed_columns_bit_identical_to_uncompressed():
+    """16-bit column storage changes only the bytes streamed, not the sums."""
+    t = torch()
+    rng = np.random.default_rng(12)
+    cases = [O.fe_matrix(3, 10, 10, 10, 3, value_mode=1, seed=3), O.fe_matrix(2, 70, 70, 0, 1, value_mode=0),
+             random_csr(rng, 200_000, 30, p_empty=0.1)]  # random columns: wide warps
+    for rp, cols, vals in cases:
+        n = len(rp) - 1
+        x = rng.uniform(-1, 1, n)
+        for kind, th in ((1, 0), (2, 5)):
+            for dtype, tdt in (("f64", t.float64), ("f32", t.float32), ("bf16", t.bfloat16)):
+                k = wk().structure() if kind == 1 else wk().structure2()
+                k.scan(len(cols), n, None, rp, None, *(() if kind == 1 else (th,)))
+                dv = wk().fe.convert(t.from_numpy(vals).cuda(), tdt)
+                eng = wk().engine(k, dv, t.from_numpy(cols).cuda(), dtype=dtype)
+                dx = wk().fe.convert(t.from_numpy(x).cuda(), tdt)
+                ydt = t.float64 if dtype == "f64" else t.float32
+                y0 = t.zeros(n, dtype=ydt, device="cuda")
+                eng.run(0, 128, dx, y0, order=0)
+                wide = eng.compress_cols()
+                y1 = t.zeros(n, dtype=ydt, device="cuda")
+                eng.run(0, 128, dx, y1, order=0)
+                assert t.equal(y0, y1), (dtype, kind, wide)
+                y2 = t.zeros(n, dtype=ydt, device="cuda")
+                eng.run_x(0, 128, dx, y2, order=0)  # run_x path of the compressed kernel
+                assert bool(t.isfinite(y2).all())
+                # set_colinds rebuilds the compact storage
+                eng.device_colinds = eng.device_colinds
+                y3 = t.zeros(n, dtype=ydt, device="cuda")
+                eng.run(0, 128, dx, y3, order=0)
+                assert t.equal(y0, y3)
+        if n == 200_000:
+            assert wide > 0  # random columns leave warps in 32-bit mode

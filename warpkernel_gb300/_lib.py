@@ -38,6 +38,12 @@ class LayoutInfo(C.Structure):
                 ("nmax_per_thread", u32)]
 
 
+class CGParams(C.Structure):
+    _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("max_inner", C.c_int),
+                ("inner_tol", C.c_double), ("check_every", C.c_int), ("iters", C.c_int),
+                ("outer", C.c_int), ("relres", C.c_double), ("seconds", C.c_double)]
+
+
 SIGNATURES = {
     "wk_last_error": (C.c_size_t, [C.c_char_p, C.c_size_t]),
     "wk_version": (C.c_char_p, []),
@@ -55,11 +61,14 @@ SIGNATURES = {
     "wk_engine_get_values": (C.c_int, [vp, vp, C.c_size_t]),
     "wk_engine_get_colinds": (C.c_int, [vp, vp, C.c_size_t]),
     "wk_engine_destroy": (C.c_int, [vp]),
+    "wk_engine_compress_cols": (C.c_int, [vp, vp, _u32p]),
     "wk_run": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, _fp]),
     "wk_run_x": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, _fp]),
     "wk_run_host": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, vp]),
     "wk_residual": (C.c_int, [vp, vp, vp, vp, vp, vp]),
     "wk_residual_static": (C.c_int, [vp, vp, vp, vp, vp, vp]),
+    "wk_cg": (C.c_int, [vp, vp, vp, C.POINTER(CGParams), vp]),
+    "wk_ir_cg": (C.c_int, [vp, vp, vp, vp, C.POINTER(CGParams), vp]),
     "wk_verify": (C.c_int, [vp, vp, vp, _ip, _i64p]),
     "wk_verify_x": (C.c_int, [vp, vp, vp, C.c_int, _ip, _i64p]),
     "wk_fe_size": (C.c_int, [C.c_int] * 5 + [_i64p, _i64p]),

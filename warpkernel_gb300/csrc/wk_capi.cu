@@ -311,6 +311,7 @@ wk_status wk_engine_set_colinds(wk_engine *e, const int32_t *padded_cols, void *
   if (bad) return set_error(WK_ERR_INVALID, "%d column indices lie outside [0, %u)", bad, e->ncols);
   if (anz) WK_CUDA(cudaMemcpyAsync(e->cols.p, c.dptr, anz * 4, cudaMemcpyDeviceToDevice, st));
   WK_CUDA(cudaStreamSynchronize(st));
+  if (e->compressed) WK_TRY(build_compressed_cols(e, st, nullptr));
   return WK_OK;
 }
 

@@ -121,6 +121,10 @@ struct wk_engine {
   wk::DevBuf status; // device status word for kernels that can report errors
   wk::DevBuf xbuf, ybuf;  // staging vectors of wk_run_host (allocated on first use)
   wk::DevBuf scratch;     // per-block partial sums of the solver kernels (grown on demand)
+  // compressed columns (wk_engine_compress_cols): 16-bit offsets per slot,
+  // compact 32-bit indices of the warps whose span needs them, per-warp descriptor
+  bool compressed = false;
+  wk::DevBuf c16, c32, cdesc;
 };
 
 namespace wk {
@@ -141,6 +145,13 @@ wk_status launch_reorder_x(const wk_layout *l, const void *x, void *xout, int el
 // Counts column indices outside [0, ncols) into *d_bad (device int).
 wk_status launch_check_cols(const int32_t *cols, size_t n, uint32_t ncols, int *d_bad,
                             cudaStream_t stream);
+
+// Exclusive scan of n uint64 values (out may alias in); *d_total = the sum.
+// Synchronises `stream`.
+wk_status scan_u64(const unsigned long long *in, unsigned long long *out, size_t n,
+                   unsigned long long *d_total, cudaStream_t stream);
+// Builds / refreshes the engine's 16-bit column storage from its int32 columns.
+wk_status build_compressed_cols(wk_engine *e, cudaStream_t stream, uint32_t *wide_warps);
 
 struct RunArgs {
   const wk_engine *e;

@@ -606,4 +606,9 @@ wk_status launch_check_cols(const int32_t *cols, size_t n, uint32_t ncols, int *
   return WK_OK;
 }
 
+wk_status scan_u64(const unsigned long long *in, unsigned long long *out, size_t n, unsigned long long *d_total,
+                   cudaStream_t st) {
+  return exclusive_scan<unsigned long long>(in, out, n, d_total, st);
+}
+
 }  // namespace wk

@@ -58,6 +58,25 @@ __global__ void __launch_bounds__(1024) k_spmv_fast(const V *__restrict__ pv, co
   if (p < nzr && (lane & (T - 1)) == 0) store_row<typename Tr<V>::Acc, MAPPED>(y, row_map, p, s);
 }
 
+// Fast order with the 16-bit column storage of wk_engine_compress_cols.
+template <typename V, typename X, bool MAPPED, bool L1>
+__global__ void __launch_bounds__(1024) k_spmv_fast_c(const V *__restrict__ pv, const uint16_t *__restrict__ c16,
+                                                      const int32_t *__restrict__ c32, const int4 *__restrict__ cdesc,
+                                                      const int4 *__restrict__ desc, uint32_t W,
+                                                      const int32_t *__restrict__ row_map, uint32_t nzr,
+                                                      const X *__restrict__ x, typename Tr<V>::Acc *__restrict__ y) {
+  const uint32_t lane = threadIdx.x & 31;
+  const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
+  if (w >= W) return;
+  const int4 d = desc[w];
+  const int4 cd = cdesc[w];
+  const uint32_t T = (uint32_t)d.z;
+  typename Tr<V>::Acc s = lane_sum_compressed<V, X, L1>(pv, c16, c32, d, cd, x, lane, policy_evict_first());
+  const uint32_t p = (uint32_t)d.w + lane / T;
+  s = row_tree(s, T);
+  if (p < nzr && (lane & (T - 1)) == 0) store_row<typename Tr<V>::Acc, MAPPED>(y, row_map, p, s);
+}
+
 template <typename V, typename X>
 wk_status dispatch(const RunArgs &a, unsigned grid, unsigned block) {
   const wk_engine *e = a.e;
@@ -72,6 +91,20 @@ wk_status dispatch(const RunArgs &a, unsigned grid, unsigned block) {
   const uint32_t W = l->info.nwarps, nzr = l->info.nznrows;
 #define WK_LAUNCH(K, M, C) K<V, X, M, C><<<grid, block, 0, a.stream>>>(pv, pc, desc, W, rm, nzr, x, y)
   const bool c = a.cache != 0;
+  if (e->compressed && a.order == WK_ORDER_FAST) {
+    const uint16_t *c16 = e->c16.as<uint16_t>();
+    const int32_t *c32 = e->c32.as<int32_t>();
+    const int4 *cd = e->cdesc.as<int4>();
+#define WK_LAUNCH_C(M, C) k_spmv_fast_c<V, X, M, C><<<grid, block, 0, a.stream>>>(pv, c16, c32, cd, desc, W, rm, nzr, x, y)
+    if (a.mapped) {
+      if (c) WK_LAUNCH_C(true, true); else WK_LAUNCH_C(true, false);
+    } else {
+      if (c) WK_LAUNCH_C(false, true); else WK_LAUNCH_C(false, false);
+    }
+#undef WK_LAUNCH_C
+    WK_CHECK_LAUNCH();
+    return WK_OK;
+  }
   if (a.order == WK_ORDER_EXACT) {
     if (a.mapped) {
       if (c) WK_LAUNCH(k_spmv_exact, true, true); else WK_LAUNCH(k_spmv_exact, true, false);

@@ -188,5 +188,93 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_fast(const V *__restrict
   return s + tail;
 }
 
+// ---- compressed column indices ---------------------------------------------------
+// A layout warp whose column indices span less than 65,536 stores them as
+// 16-bit offsets from a per-warp base (2 bytes per slot instead of 4); other
+// warps keep 32-bit indices in a compact side array.  cdesc = {base, mode
+// (0 = 16-bit, 1 = 32-bit), offset of the warp in the 32-bit array, 0}.
+__device__ __forceinline__ void ld_stream4(const uint16_t *p, int (&c)[4], int base, uint64_t pol) {
+  unsigned a, b;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.b32 {%0,%1}, [%2], %3;"
+               : "=r"(a), "=r"(b)
+               : "l"(p), "l"(pol));
+  c[0] = base + (int)(a & 0xffffu);
+  c[1] = base + (int)(a >> 16);
+  c[2] = base + (int)(b & 0xffffu);
+  c[3] = base + (int)(b >> 16);
+}
+__device__ __forceinline__ int ld_stream1(const uint16_t *p, int base, uint64_t pol) {
+  unsigned short v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(v) : "l"(p), "l"(pol));
+  return base + (int)v;
+}
+
+template <typename V, typename X, bool L1, typename C>
+__device__ __forceinline__ typename Tr<V>::Acc lane_sum_fast_cols(const V *__restrict__ pv, const C *__restrict__ cp0,
+                                                                 int base, int4 d, const X *__restrict__ x,
+                                                                 uint32_t lane, uint64_t pol) {
+  typedef typename Tr<V>::Acc Acc;
+  const uint32_t A = (uint32_t)d.y;
+  const size_t o = (size_t)(uint32_t)d.x;
+  const uint32_t units = A >> 2, rem = A & 3u;
+  Acc a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+  const V *vp = pv + o + 4 * lane;
+  const C *cp = cp0 + 4 * lane;
+#pragma unroll 2
+  for (uint32_t u = 0; u < units; u++) {
+    V v[4];
+    int c[4];
+    ld_stream(vp, v, pol);
+    if constexpr (sizeof(C) == 2)
+      ld_stream4(cp, c, base, pol);
+    else
+      ld_stream4(cp, c, pol);
+    a0 = fma_acc(Tr<V>::acc(v[0]), (Acc)Tr<X>::acc(gather<L1>(x, c[0])), a0);
+    a1 = fma_acc(Tr<V>::acc(v[1]), (Acc)Tr<X>::acc(gather<L1>(x, c[1])), a1);
+    a2 = fma_acc(Tr<V>::acc(v[2]), (Acc)Tr<X>::acc(gather<L1>(x, c[2])), a2);
+    a3 = fma_acc(Tr<V>::acc(v[3]), (Acc)Tr<X>::acc(gather<L1>(x, c[3])), a3);
+    vp += 4 * WS;
+    cp += 4 * WS;
+  }
+  Acc tail = Acc(0);
+  const size_t ut = (size_t)units * 4 * WS + lane;
+  for (uint32_t i = 0; i < rem; i++) {
+    int c;
+    if constexpr (sizeof(C) == 2)
+      c = ld_stream1(cp0 + ut + (size_t)i * WS, base, pol);
+    else
+      c = ld_stream1(cp0 + ut + (size_t)i * WS, pol);
+    tail = fma_acc(Tr<V>::acc(ld_stream1(pv + o + ut + (size_t)i * WS, pol)), (Acc)Tr<X>::acc(gather<L1>(x, c)), tail);
+  }
+  a0 += __shfl_xor_sync(0xffffffffu, a0, 8);
+  a1 += __shfl_xor_sync(0xffffffffu, a1, 8);
+  a2 += __shfl_xor_sync(0xffffffffu, a2, 8);
+  a3 += __shfl_xor_sync(0xffffffffu, a3, 8);
+  a0 += __shfl_xor_sync(0xffffffffu, a0, 16);
+  a1 += __shfl_xor_sync(0xffffffffu, a1, 16);
+  a2 += __shfl_xor_sync(0xffffffffu, a2, 16);
+  a3 += __shfl_xor_sync(0xffffffffu, a3, 16);
+  const int src = (int)(lane >> 2);
+  Acc t0 = __shfl_sync(0xffffffffu, a0, src);
+  Acc t1 = __shfl_sync(0xffffffffu, a1, src);
+  Acc t2 = __shfl_sync(0xffffffffu, a2, src);
+  Acc t3 = __shfl_sync(0xffffffffu, a3, src);
+  const uint32_t k = lane & 3u;
+  Acc s = k == 0 ? t0 : k == 1 ? t1 : k == 2 ? t2 : t3;
+  return s + tail;
+}
+
+// Row sums with compressed columns: c16 is indexed by slot, c32 by the warp's
+// compact offset (cdesc.z) plus the slot's position in the warp.
+template <typename V, typename X, bool L1>
+__device__ __forceinline__ typename Tr<V>::Acc lane_sum_compressed(const V *__restrict__ pv,
+                                                                  const uint16_t *__restrict__ c16,
+                                                                  const int32_t *__restrict__ c32, int4 d,
+                                                                  int4 cd, const X *__restrict__ x,
+                                                                  uint32_t lane, uint64_t pol) {
+  if (cd.y == 0) return lane_sum_fast_cols<V, X, L1, uint16_t>(pv, c16 + (uint32_t)d.x, cd.x, d, x, lane, pol);
+  return lane_sum_fast_cols<V, X, L1, int32_t>(pv, c32 + (uint32_t)cd.z, 0, d, x, lane, pol);
+}
+
 }  // namespace core
 }  // namespace wk

@@ -258,6 +258,13 @@ class engine:
         check(load().wk_engine_get_values(self.handle, a.ctypes.data, a.size))
         return a
 
+    def compress_cols(self, stream=None):
+        """16-bit column offsets for warps spanning < 65,536 columns (fast
+        order); returns the number of warps left with 32-bit indices."""
+        wide = C.c_uint32(0)
+        check(load().wk_engine_compress_cols(self.handle, _stream_ptr(stream), C.byref(wide)))
+        return int(wide.value)
+
     def set_values(self, A, stream=None):
         check(load().wk_engine_set_values(self.handle, _ptr(A), _stream_ptr(stream)))
 
@@ -309,6 +316,37 @@ class engine:
         check(load().wk_verify_x(self.kernel.handle, o.ctypes.data, c.ctypes.data, int(strict), C.byref(ok),
                                  C.byref(bad)))
         return bool(ok.value)
+
+
+def _cg_params(tol, max_iter, max_inner, inner_tol, check_every):
+    p = _lib.CGParams()
+    p.tol, p.max_iter, p.max_inner, p.inner_tol, p.check_every = tol, max_iter, max_inner, inner_tol, check_every
+    return p
+
+
+def _cg_result(p, status):
+    res = {"iters": p.iters, "outer": p.outer, "relres": p.relres, "seconds": p.seconds,
+           "converged": status == 0}
+    if status not in (0, 7):  # WK_ERR_NOTCONV is reported in the result
+        check(status)
+    return res
+
+
+def cg(eng64, b, x, tol=1e-10, max_iter=100000, check_every=10, stream=None):
+    """fp64 conjugate gradient on an fp64 engine (device vectors b, x; x is
+    the initial guess and is overwritten)."""
+    p = _cg_params(tol, max_iter, 0, 0.0, check_every)
+    st = load().wk_cg(eng64.handle, _ptr(b), _ptr(x), C.byref(p), _stream_ptr(stream))
+    return _cg_result(p, st)
+
+
+def ir_cg(eng64, eng_lo, b, x, tol=1e-10, max_outer=50, max_inner=2000, inner_tol=1e-4, check_every=10,
+          stream=None):
+    """Iterative refinement: fp64 residual / dots / update, fp32 inner CG on
+    the low-precision engine (WK_F32 or WK_BF16 values)."""
+    p = _cg_params(tol, max_outer, max_inner, inner_tol, check_every)
+    st = load().wk_ir_cg(eng64.handle, eng_lo.handle, _ptr(b), _ptr(x), C.byref(p), _stream_ptr(stream))
+    return _cg_result(p, st)
 
 
 class profiler:
