@@ -1,0 +1,399 @@
+// wk_cg.cu -- conjugate gradient (fp64) and iterative-refinement CG (fp64
+// outer loop, fp32 inner CG on an FP32 / BF16 engine) on the WPK layout.
+//
+// All scalars stay on the device.  Each reduction writes block partials that
+// a one-block kernel sums in a fixed order into a slot of `scal`, so results
+// are bit-reproducible.  The kernel that finishes r.r also sets a done flag
+// (converged, or the iteration limit reached); every CG kernel returns at
+// once when the flag is set.  A batch of iterations is captured once in a
+// CUDA graph and replayed; the host reads the flag after each batch.
+#include <algorithm>
+#include <cmath>
+
+#include "wk_internal.cuh"
+#include "wk_spmv_core.cuh"
+
+namespace wk {
+namespace {
+
+using namespace core;
+
+constexpr int CG_BLOCK = 128;              // 4 warps per block in the SpMV-dot kernel
+constexpr unsigned CG_GRID = 152 * 12;     // blocks of the SpMV-dot kernel (grid-stride over layout warps)
+constexpr int VEC_BLOCK = 256;
+constexpr unsigned VEC_GRID = 152 * 8;     // blocks of the vector kernels
+constexpr unsigned MAX_PARTIALS = CG_GRID > VEC_GRID ? CG_GRID : VEC_GRID;
+
+// slots of `scal`
+enum { S_RHO0, S_RHO1, S_PQ, S_BB, S_RR64, S_TOL2, S_DONE, S_ITERS, S_MAXIT, S_COUNT };
+
+__device__ __forceinline__ bool done(const double *scal) { return scal[S_DONE] != 0.0; }
+__device__ __forceinline__ double safe_div(double a, double b) { return b != 0.0 ? a / b : 0.0; }
+
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int off = 16; off; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  if (lane == 0) sh[wib] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (wib == 0) {
+    t = lane < nw ? sh[lane] : 0.0;
+#pragma unroll
+    for (int off = 16; off; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+  }
+  return t;  // valid in thread 0
+}
+
+// q = A p (rows without entries get 0) and block partials of p . q
+template <typename V, typename X, bool COMP>
+__global__ void __launch_bounds__(CG_BLOCK) k_spmv_dot(const V *__restrict__ pv, const int32_t *__restrict__ pc,
+                                                       const uint16_t *__restrict__ c16, const int32_t *__restrict__ c32,
+                                                       const int4 *__restrict__ cdesc, const int4 *__restrict__ desc,
+                                                       uint32_t W, const int32_t *__restrict__ row_map, uint32_t nzr,
+                                                       uint32_t nrows, const X *__restrict__ p, X *__restrict__ q,
+                                                       const double *__restrict__ scal, double *__restrict__ partials) {
+  if (done(scal)) return;
+  __shared__ double sh[32];
+  const uint32_t lane = threadIdx.x & 31;
+  const size_t nw = (size_t)gridDim.x * blockDim.x / WS;
+  double part = 0.0;
+  const uint64_t pol = policy_evict_first();
+  for (size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS; w < W; w += nw) {
+    const int4 d = desc[w];
+    const uint32_t T = (uint32_t)d.z;
+    typename Tr<V>::Acc s;
+    if constexpr (COMP)
+      s = lane_sum_compressed<V, X, true>(pv, c16, c32, d, cdesc[w], p, lane, pol);
+    else
+      s = lane_sum_fast<V, X, true>(pv, pc, d, p, lane, pol);
+    s = row_tree(s, T);
+    const uint32_t r = (uint32_t)d.w + lane / T;
+    if (r < nzr && (lane & (T - 1)) == 0) {
+      const int32_t row = row_map[r];
+      const X qv = (X)s;
+      q[row] = qv;
+      part = fma((double)p[row], (double)qv, part);
+    }
+  }
+  for (size_t k = (size_t)nzr + (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nrows;
+       k += (size_t)gridDim.x * blockDim.x)
+    q[row_map[k]] = X(0);
+  const double t = block_sum(part, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = t;
+}
+
+// scal[out] = fixed-order sum of partials[0..n); with CHECK also counts the
+// iteration and sets the done flag (1: r.r <= tol2, 2: iteration limit).
+template <bool CHECK>
+__global__ void __launch_bounds__(1024) k_finish(const double *__restrict__ partials, unsigned n, double *scal,
+                                                 int out) {
+  if (done(scal)) return;
+  __shared__ double sh[32];
+  double v = 0.0;
+  for (unsigned i = threadIdx.x; i < n; i += blockDim.x) v += partials[i];
+  const double t = block_sum(v, sh);
+  if (threadIdx.x == 0) {
+    scal[out] = t;
+    if (CHECK) {
+      const double it = scal[S_ITERS] + 1.0;
+      scal[S_ITERS] = it;
+      if (t <= scal[S_TOL2])
+        scal[S_DONE] = 1.0;
+      else if (it >= scal[S_MAXIT])
+        scal[S_DONE] = 2.0;
+    }
+  }
+}
+
+// x += alpha p, r -= alpha q, partials of r . r; alpha = scal[rho] / scal[pq]
+template <typename T>
+__global__ void __launch_bounds__(VEC_BLOCK) k_update(T *__restrict__ x, T *__restrict__ r, const T *__restrict__ p,
+                                                      const T *__restrict__ q, uint32_t n, const double *__restrict__ scal,
+                                                      int i_rho, double *__restrict__ partials) {
+  if (done(scal)) return;
+  __shared__ double sh[32];
+  const double alpha = safe_div(scal[i_rho], scal[S_PQ]);
+  double part = 0.0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const T ri = (T)((double)r[i] - alpha * (double)q[i]);
+    x[i] = (T)((double)x[i] + alpha * (double)p[i]);
+    r[i] = ri;
+    part = fma((double)ri, (double)ri, part);
+  }
+  const double t = block_sum(part, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = t;
+}
+
+// p = r + beta p, beta = scal[rr] / scal[rho]
+template <typename T>
+__global__ void __launch_bounds__(VEC_BLOCK) k_pupdate(T *__restrict__ p, const T *__restrict__ r, uint32_t n,
+                                                       const double *__restrict__ scal, int i_rr, int i_rho) {
+  if (done(scal)) return;
+  const double beta = safe_div(scal[i_rr], scal[i_rho]);
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    p[i] = (T)((double)r[i] + beta * (double)p[i]);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(VEC_BLOCK) k_dot_self(const T *__restrict__ a, uint32_t n,
+                                                        double *__restrict__ partials) {
+  __shared__ double sh[32];
+  double part = 0.0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    part = fma((double)a[i], (double)a[i], part);
+  const double t = block_sum(part, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = t;
+}
+
+__global__ void k_sum_to(const double *__restrict__ partials, unsigned n, double *out) {
+  __shared__ double sh[32];
+  double v = 0.0;
+  for (unsigned i = threadIdx.x; i < n; i += blockDim.x) v += partials[i];
+  const double t = block_sum(v, sh);
+  if (threadIdx.x == 0) *out = t;
+}
+
+// Start of a CG run: tol2 = tol^2 * scal[ref]; counters cleared.
+__global__ void k_start(double *scal, int ref, double tol_sq, double maxit) {
+  scal[S_TOL2] = tol_sq * scal[ref];
+  scal[S_ITERS] = 0.0;
+  scal[S_MAXIT] = maxit;
+  scal[S_DONE] = scal[S_RHO0] <= scal[S_TOL2] ? 1.0 : 0.0;
+}
+
+// IR: r32 = r64, d = 0, p = r32
+__global__ void __launch_bounds__(VEC_BLOCK) k_ir_prepare(const double *__restrict__ r64, float *__restrict__ r32,
+                                                          float *__restrict__ d, float *__restrict__ p, uint32_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float v = (float)r64[i];
+    r32[i] = v;
+    p[i] = v;
+    d[i] = 0.f;
+  }
+}
+
+// IR: x64 += d
+__global__ void __launch_bounds__(VEC_BLOCK) k_ir_correct(double *__restrict__ x, const float *__restrict__ d,
+                                                          uint32_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    x[i] += (double)d[i];
+}
+
+template <typename X>
+struct CgVectors {
+  X *x, *r, *p, *q;
+};
+
+// One CG iteration; `parity` selects which rho slot is current.
+template <typename X>
+void cg_iteration(const wk_engine *e, const CgVectors<X> &v, double *scal, double *partials, int parity,
+                  cudaStream_t st) {
+  const wk_layout *l = e->layout;
+  const uint32_t W = l->info.nwarps, n = l->info.nrows;
+  const unsigned g = std::max(1u, std::min(CG_GRID, (unsigned)((W + CG_BLOCK / WS - 1) / (CG_BLOCK / WS))));
+  const int i_rho = parity ? S_RHO1 : S_RHO0, i_next = parity ? S_RHO0 : S_RHO1;
+#define WK_SPMV_DOT(V, COMP)                                                                                        \
+  k_spmv_dot<V, X, COMP><<<g, CG_BLOCK, 0, st>>>(e->vals.as<V>(), e->cols.as<int32_t>(), e->c16.as<uint16_t>(),      \
+                                                 e->c32.as<int32_t>(), e->cdesc.as<int4>(), l->d.warp_desc, W,        \
+                                                 l->d.row_map, l->info.nznrows, n, v.p, v.q, scal, partials)
+  if constexpr (sizeof(X) == 8) {
+    if (e->compressed) WK_SPMV_DOT(double, true); else WK_SPMV_DOT(double, false);
+  } else {
+    if (e->dtype == WK_F32) {
+      if (e->compressed) WK_SPMV_DOT(float, true); else WK_SPMV_DOT(float, false);
+    } else {
+      if (e->compressed) WK_SPMV_DOT(__nv_bfloat16, true); else WK_SPMV_DOT(__nv_bfloat16, false);
+    }
+  }
+#undef WK_SPMV_DOT
+  k_finish<false><<<1, 1024, 0, st>>>(partials, g, scal, S_PQ);
+  k_update<X><<<VEC_GRID, VEC_BLOCK, 0, st>>>(v.x, v.r, v.p, v.q, n, scal, i_rho, partials);
+  k_finish<true><<<1, 1024, 0, st>>>(partials, VEC_GRID, scal, i_next);
+  k_pupdate<X><<<VEC_GRID, VEC_BLOCK, 0, st>>>(v.p, v.r, n, scal, i_next, i_rho);
+}
+
+template <typename X>
+wk_status dot_self(const X *a, uint32_t n, double *partials, double *out, cudaStream_t st) {
+  k_dot_self<X><<<VEC_GRID, VEC_BLOCK, 0, st>>>(a, n, partials);
+  k_sum_to<<<1, 1024, 0, st>>>(partials, VEC_GRID, out);
+  WK_CHECK_LAUNCH();
+  return WK_OK;
+}
+
+// A batch of `iters` (even) CG iterations captured once as a CUDA graph.
+struct IterGraph {
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t cap = nullptr;
+  ~IterGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (cap) cudaStreamDestroy(cap);
+  }
+  template <typename X>
+  wk_status build(const wk_engine *e, const CgVectors<X> &v, double *scal, double *partials, int iters) {
+    WK_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    WK_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    for (int i = 0; i < iters; i++) cg_iteration<X>(e, v, scal, partials, i & 1, cap);
+    cudaGraph_t g = nullptr;
+    cudaError_t err = cudaStreamEndCapture(cap, &g);
+    if (err != cudaSuccess) {
+      cudaGetLastError();
+      return set_error(WK_ERR_CUDA, "CG graph capture failed: %s", cudaGetErrorString(err));
+    }
+    err = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    if (err != cudaSuccess) return set_error(WK_ERR_CUDA, "CG graph instantiation failed: %s", cudaGetErrorString(err));
+    return WK_OK;
+  }
+};
+
+// Replays the graph until the done flag is set; returns the iteration count.
+wk_status run_until_done(IterGraph &gr, double *scal, cudaStream_t st, int *iters, int *flag) {
+  double h[2] = {0, 0};
+  for (;;) {
+    WK_CUDA(cudaGraphLaunch(gr.exec, st));
+    WK_CUDA(cudaMemcpyAsync(h, scal + S_DONE, 16, cudaMemcpyDeviceToHost, st));  // S_DONE, S_ITERS
+    WK_CUDA(cudaStreamSynchronize(st));
+    if (h[0] != 0.0) break;
+  }
+  *iters = (int)h[1];
+  *flag = (int)h[0];
+  return WK_OK;
+}
+
+wk_status check_square(const wk_engine *e) {
+  if (e->ncols != e->layout->info.nrows)
+    return set_error(WK_ERR_INVALID, "CG needs a square matrix (ncols %u, nrows %u)", e->ncols, e->layout->info.nrows);
+  return WK_OK;
+}
+
+int batch_of(const wk_cg_params *p) {
+  int b = p->check_every > 0 ? p->check_every : 16;
+  return b + (b & 1);  // even: the rho slots alternate
+}
+
+}  // namespace
+}  // namespace wk
+
+using namespace wk;
+
+extern "C" wk_status wk_cg(wk_engine *e, const double *b, double *x, wk_cg_params *prm, void *stream) {
+  if (!e || !b || !x || !prm) return set_error(WK_ERR_INVALID, "NULL argument");
+  if (e->dtype != WK_F64) return set_error(WK_ERR_INVALID, "wk_cg needs a WK_F64 engine");
+  WK_TRY(check_square(e));
+  if (prm->max_iter <= 0) return set_error(WK_ERR_INVALID, "max_iter must be positive");
+  cudaStream_t st = (cudaStream_t)stream;
+  const uint32_t n = e->layout->info.nrows;
+  const unsigned rg = residual_grid(e->layout);
+  DevBuf rb, pb, qb, sb, part;
+  WK_TRY(rb.alloc((size_t)n * 8));
+  WK_TRY(pb.alloc((size_t)n * 8));
+  WK_TRY(qb.alloc((size_t)n * 8));
+  WK_TRY(sb.alloc(S_COUNT * 8));
+  WK_TRY(part.alloc((size_t)std::max(rg, MAX_PARTIALS) * 8));
+  double *scal = sb.as<double>(), *pp = part.as<double>();
+  CgVectors<double> v{x, rb.as<double>(), pb.as<double>(), qb.as<double>()};
+  IterGraph gr;
+  WK_TRY(gr.build<double>(e, v, scal, pp, batch_of(prm)));
+  cudaEvent_t t0, t1;
+  WK_CUDA(cudaEventCreate(&t0));
+  WK_CUDA(cudaEventCreate(&t1));
+  WK_CUDA(cudaEventRecord(t0, st));
+  WK_TRY(dot_self<double>(b, n, pp, scal + S_BB, st));
+  WK_TRY(launch_residual(e, x, b, v.r, pp, rg, scal + S_RHO0, st));
+  WK_CUDA(cudaMemcpyAsync(v.p, v.r, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+  k_start<<<1, 1, 0, st>>>(scal, S_BB, prm->tol * prm->tol, (double)prm->max_iter);
+  WK_CHECK_LAUNCH();
+  int iters = 0, flag = 0;
+  WK_TRY(run_until_done(gr, scal, st, &iters, &flag));
+  WK_TRY(launch_residual(e, x, b, v.r, pp, rg, scal + S_RR64, st));  // true residual of the result
+  WK_CUDA(cudaEventRecord(t1, st));
+  double h[2];
+  WK_CUDA(cudaMemcpyAsync(&h[0], scal + S_RR64, 8, cudaMemcpyDeviceToHost, st));
+  WK_CUDA(cudaMemcpyAsync(&h[1], scal + S_BB, 8, cudaMemcpyDeviceToHost, st));
+  WK_CUDA(cudaStreamSynchronize(st));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, t0, t1);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  const double bb = h[1] > 0 ? h[1] : 1.0;
+  prm->iters = iters;
+  prm->outer = 0;
+  prm->relres = std::sqrt(h[0] / bb);
+  prm->seconds = ms * 1e-3;
+  if (prm->relres <= prm->tol) return WK_OK;
+  return set_error(WK_ERR_NOTCONV, "CG stopped after %d iterations at relative residual %.3e", iters, prm->relres);
+}
+
+extern "C" wk_status wk_ir_cg(wk_engine *e64, wk_engine *lo, const double *b, double *x, wk_cg_params *prm,
+                              void *stream) {
+  if (!e64 || !lo || !b || !x || !prm) return set_error(WK_ERR_INVALID, "NULL argument");
+  if (e64->dtype != WK_F64) return set_error(WK_ERR_INVALID, "wk_ir_cg: the residual engine must be WK_F64");
+  if (lo->dtype != WK_F32 && lo->dtype != WK_BF16)
+    return set_error(WK_ERR_INVALID, "wk_ir_cg: the inner engine must be WK_F32 or WK_BF16");
+  WK_TRY(check_square(e64));
+  if (lo->layout->info.nrows != e64->layout->info.nrows || lo->ncols != e64->ncols)
+    return set_error(WK_ERR_INVALID, "wk_ir_cg: engines of different sizes");
+  if (prm->max_iter <= 0) return set_error(WK_ERR_INVALID, "max_iter must be positive");
+  cudaStream_t st = (cudaStream_t)stream;
+  const uint32_t n = e64->layout->info.nrows;
+  const int max_inner = prm->max_inner > 0 ? prm->max_inner : 1000;
+  const double inner_tol = prm->inner_tol > 0 ? prm->inner_tol : 1e-4;
+  const unsigned rg = residual_grid(e64->layout);
+  DevBuf r64b, r32b, db, pb, qb, sb, part;
+  WK_TRY(r64b.alloc((size_t)n * 8));
+  WK_TRY(r32b.alloc((size_t)n * 4));
+  WK_TRY(db.alloc((size_t)n * 4));
+  WK_TRY(pb.alloc((size_t)n * 4));
+  WK_TRY(qb.alloc((size_t)n * 4));
+  WK_TRY(sb.alloc(S_COUNT * 8));
+  WK_TRY(part.alloc((size_t)std::max(rg, MAX_PARTIALS) * 8));
+  double *r64 = r64b.as<double>(), *scal = sb.as<double>(), *pp = part.as<double>();
+  CgVectors<float> v{db.as<float>(), r32b.as<float>(), pb.as<float>(), qb.as<float>()};
+  IterGraph gr;
+  WK_TRY(gr.build<float>(lo, v, scal, pp, batch_of(prm)));
+  cudaEvent_t t0, t1;
+  WK_CUDA(cudaEventCreate(&t0));
+  WK_CUDA(cudaEventCreate(&t1));
+  WK_CUDA(cudaEventRecord(t0, st));
+  WK_TRY(dot_self<double>(b, n, pp, scal + S_BB, st));
+  double bb = 0.0;
+  WK_CUDA(cudaMemcpyAsync(&bb, scal + S_BB, 8, cudaMemcpyDeviceToHost, st));
+  WK_CUDA(cudaStreamSynchronize(st));
+  if (!(bb > 0)) bb = 1.0;
+  const double tol2 = prm->tol * prm->tol * bb;
+  int outer = 0, inner_total = 0;
+  double rr64 = 0.0;
+  for (;;) {
+    // fp64: r = b - A x and ||r||^2
+    WK_TRY(launch_residual(e64, x, b, r64, pp, rg, scal + S_RR64, st));
+    WK_CUDA(cudaMemcpyAsync(&rr64, scal + S_RR64, 8, cudaMemcpyDeviceToHost, st));
+    WK_CUDA(cudaStreamSynchronize(st));
+    if (!(rr64 > tol2) || outer >= prm->max_iter) break;
+    // fp32 inner CG: A d = r from d = 0 until ||r_inner|| <= inner_tol ||r||
+    k_ir_prepare<<<VEC_GRID, VEC_BLOCK, 0, st>>>(r64, v.r, v.x, v.p, n);
+    WK_TRY(dot_self<float>(v.r, n, pp, scal + S_RHO0, st));
+    k_start<<<1, 1, 0, st>>>(scal, S_RHO0, inner_tol * inner_tol, (double)max_inner);
+    WK_CHECK_LAUNCH();
+    int its = 0, flag = 0;
+    WK_TRY(run_until_done(gr, scal, st, &its, &flag));
+    inner_total += its;
+    // fp64 update
+    k_ir_correct<<<VEC_GRID, VEC_BLOCK, 0, st>>>(x, v.x, n);
+    WK_CHECK_LAUNCH();
+    outer++;
+  }
+  WK_CUDA(cudaEventRecord(t1, st));
+  WK_CUDA(cudaEventSynchronize(t1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, t0, t1);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  prm->iters = inner_total;
+  prm->outer = outer;
+  prm->relres = std::sqrt(rr64 / bb);
+  prm->seconds = ms * 1e-3;
+  if (prm->relres <= prm->tol) return WK_OK;
+  return set_error(WK_ERR_NOTCONV, "IR-CG stopped after %d outer / %d inner iterations at %.3e", outer, inner_total,
+                   prm->relres);
+}

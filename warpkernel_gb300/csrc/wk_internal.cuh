@@ -153,6 +153,12 @@ wk_status scan_u64(const unsigned long long *in, unsigned long long *out, size_t
 // Builds / refreshes the engine's 16-bit column storage from its int32 columns.
 wk_status build_compressed_cols(wk_engine *e, cudaStream_t stream, uint32_t *wide_warps);
 
+// fp64 residual r = b - A x with block partials of ||r||^2 (wk_solve.cu);
+// norm2 (device, optional) receives their fixed-order sum.
+unsigned residual_grid(const wk_layout *l);
+wk_status launch_residual(const wk_engine *e, const double *x, const double *b, double *r, double *partials,
+                          unsigned grid, double *norm2, cudaStream_t stream);
+
 struct RunArgs {
   const wk_engine *e;
   int nblocks, blocksize, cache, order;

@@ -133,59 +133,123 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_exact(const V *__restric
   return s;
 }
 
-// Fast order: each lane streams 4 consecutive slots of a 4-step unit (slots
-// 4j..4j+3 = layout lanes 4(j%8)..4(j%8)+3 at step j/8) with one 256-bit
-// (fp64), 128-bit (fp32) or 64-bit (bf16) value load and one 128-bit column
-// load; partials are combined across the four lanes holding the same layout
-// lanes (xor 8, xor 16) and moved to the owning lane; the A_w % 4 remaining
+// ---- word loads (streaming) and unpacking ----------------------------------------
+__device__ __forceinline__ void ld_words(const void *p, uint32_t (&w)[2], uint64_t pol) {
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.b32 {%0,%1}, [%2], %3;"
+               : "=r"(w[0]), "=r"(w[1])
+               : "l"(p), "l"(pol));
+}
+__device__ __forceinline__ void ld_words(const void *p, uint32_t (&w)[4], uint64_t pol) {
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.b32 {%0,%1,%2,%3}, [%4], %5;"
+               : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3])
+               : "l"(p), "l"(pol));
+}
+__device__ __forceinline__ void ld_words(const void *p, uint32_t (&w)[8], uint64_t pol) {
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8], %9;"
+               : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]), "=r"(w[6]), "=r"(w[7])
+               : "l"(p), "l"(pol));
+}
+template <typename V>
+__device__ __forceinline__ V word_val(const uint32_t *w, int k);
+template <>
+__device__ __forceinline__ double word_val<double>(const uint32_t *w, int k) {
+  return __hiloint2double((int)w[2 * k + 1], (int)w[2 * k]);
+}
+template <>
+__device__ __forceinline__ float word_val<float>(const uint32_t *w, int k) {
+  return __uint_as_float(w[k]);
+}
+template <>
+__device__ __forceinline__ __nv_bfloat16 word_val<__nv_bfloat16>(const uint32_t *w, int k) {
+  return __ushort_as_bfloat16((unsigned short)((k & 1) ? (w[k >> 1] >> 16) : (w[k >> 1] & 0xffffu)));
+}
+template <typename C>
+__device__ __forceinline__ int word_col(const uint32_t *w, int k, int base);
+template <>
+__device__ __forceinline__ int word_col<int32_t>(const uint32_t *w, int k, int) {
+  return (int)w[k];
+}
+template <>
+__device__ __forceinline__ int word_col<uint16_t>(const uint32_t *w, int k, int base) {
+  return base + (int)((k & 1) ? (w[k >> 1] >> 16) : (w[k >> 1] & 0xffffu));
+}
+__device__ __forceinline__ int ld_col1(const int32_t *p, int, uint64_t pol) { return ld_stream1(p, pol); }
+__device__ __forceinline__ int ld_col1(const uint16_t *p, int base, uint64_t pol) {
+  unsigned short v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(v) : "l"(p), "l"(pol));
+  return base + (int)v;
+}
+
+// Slots each lane streams per iteration: 32 B of values for fp64 (4 slots),
+// 32 B for fp32 and 16 B for bf16 (8 slots).
+template <typename V>
+struct SlotsPerLane {
+  static constexpr int value = sizeof(V) == 8 ? 4 : 8;
+};
+
+// Fast order: with S slots per lane, a unit of S steps is 32*S consecutive
+// slots; lane j streams slots S*j .. S*j+S-1 (layout lanes S*(j%R) .. +S-1 at
+// step j/R, R = 32/S) with one vector load of values and one of columns.
+// Partials are combined across the S lanes holding the same layout lanes
+// (xor R, 2R, ..., 16) and moved to the owning lane; the A_w % S remaining
 // steps are added one slot per lane.  Returns layout lane `lane`'s total.
-template <typename V, typename X, bool L1>
-__device__ __forceinline__ typename Tr<V>::Acc lane_sum_fast(const V *__restrict__ pv,
-                                                            const int32_t *__restrict__ pc, int4 d,
-                                                            const X *__restrict__ x, uint32_t lane,
-                                                            uint64_t pol) {
+// cp0 points at the warp's first column entry (slot o_w of a slot-indexed
+// array, or the warp's start in a compact array); base is added to 16-bit
+// offsets.
+template <typename V, typename X, bool L1, typename C>
+__device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict__ pv, const C *__restrict__ cp0, int base,
+                                                           int4 d, const X *__restrict__ x, uint32_t lane,
+                                                           uint64_t pol) {
   typedef typename Tr<V>::Acc Acc;
+  constexpr int S = SlotsPerLane<V>::value;
+  constexpr int R = 32 / S;
+  constexpr int NWV = S * (int)sizeof(V) / 4, NWC = S * (int)sizeof(C) / 4;
   const uint32_t A = (uint32_t)d.y;
   const size_t o = (size_t)(uint32_t)d.x;
-  const uint32_t units = A >> 2, rem = A & 3u;
-  Acc a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-  const V *vp = pv + o + 4 * lane;
-  const int32_t *cp = pc + o + 4 * lane;
+  const uint32_t units = A / S, rem = A % S;
+  Acc a[S];
+#pragma unroll
+  for (int k = 0; k < S; k++) a[k] = Acc(0);
+  const V *vp = pv + o + S * lane;
+  const C *cp = cp0 + S * lane;
 #pragma unroll 2
   for (uint32_t u = 0; u < units; u++) {
-    V v[4];
-    int c[4];
-    ld_stream(vp, v, pol);
-    ld_stream4(cp, c, pol);
-    a0 = fma_acc(Tr<V>::acc(v[0]), (Acc)Tr<X>::acc(gather<L1>(x, c[0])), a0);
-    a1 = fma_acc(Tr<V>::acc(v[1]), (Acc)Tr<X>::acc(gather<L1>(x, c[1])), a1);
-    a2 = fma_acc(Tr<V>::acc(v[2]), (Acc)Tr<X>::acc(gather<L1>(x, c[2])), a2);
-    a3 = fma_acc(Tr<V>::acc(v[3]), (Acc)Tr<X>::acc(gather<L1>(x, c[3])), a3);
-    vp += 4 * WS;
-    cp += 4 * WS;
+    uint32_t wv[NWV], wc[NWC];
+    ld_words(vp, wv, pol);
+    ld_words(cp, wc, pol);
+#pragma unroll
+    for (int k = 0; k < S; k++)
+      a[k] = fma_acc(Tr<V>::acc(word_val<V>(wv, k)), (Acc)Tr<X>::acc(gather<L1>(x, word_col<C>(wc, k, base))), a[k]);
+    vp += S * WS;
+    cp += S * WS;
   }
-  // remaining steps, one slot per lane (issued before the shuffles)
   Acc tail = Acc(0);
-  size_t ot = o + (size_t)units * 4 * WS + lane;
-  for (uint32_t i = 0; i < rem; i++, ot += WS)
-    tail = fma_acc(Tr<V>::acc(ld_stream1(pv + ot, pol)), (Acc)Tr<X>::acc(gather<L1>(x, ld_stream1(pc + ot, pol))),
-                   tail);
-  a0 += __shfl_xor_sync(0xffffffffu, a0, 8);
-  a1 += __shfl_xor_sync(0xffffffffu, a1, 8);
-  a2 += __shfl_xor_sync(0xffffffffu, a2, 8);
-  a3 += __shfl_xor_sync(0xffffffffu, a3, 8);
-  a0 += __shfl_xor_sync(0xffffffffu, a0, 16);
-  a1 += __shfl_xor_sync(0xffffffffu, a1, 16);
-  a2 += __shfl_xor_sync(0xffffffffu, a2, 16);
-  a3 += __shfl_xor_sync(0xffffffffu, a3, 16);
-  const int src = (int)(lane >> 2);
-  Acc t0 = __shfl_sync(0xffffffffu, a0, src);
-  Acc t1 = __shfl_sync(0xffffffffu, a1, src);
-  Acc t2 = __shfl_sync(0xffffffffu, a2, src);
-  Acc t3 = __shfl_sync(0xffffffffu, a3, src);
-  const uint32_t k = lane & 3u;
-  Acc s = k == 0 ? t0 : k == 1 ? t1 : k == 2 ? t2 : t3;
+  const size_t ut = (size_t)units * S * WS + lane;
+  for (uint32_t i = 0; i < rem; i++) {
+    const int c = ld_col1(cp0 + ut + (size_t)i * WS, base, pol);
+    tail = fma_acc(Tr<V>::acc(ld_stream1(pv + o + ut + (size_t)i * WS, pol)), (Acc)Tr<X>::acc(gather<L1>(x, c)), tail);
+  }
+#pragma unroll
+  for (int m = R; m < 32; m <<= 1) {
+#pragma unroll
+    for (int k = 0; k < S; k++) a[k] += __shfl_xor_sync(0xffffffffu, a[k], m);
+  }
+  const int src = (int)(lane / S);
+  const uint32_t kk = lane % S;
+  Acc s = Acc(0);
+#pragma unroll
+  for (int k = 0; k < S; k++) {
+    const Acc t = __shfl_sync(0xffffffffu, a[k], src);
+    if (kk == (uint32_t)k) s = t;
+  }
   return s + tail;
+}
+
+template <typename V, typename X, bool L1>
+__device__ __forceinline__ typename Tr<V>::Acc lane_sum_fast(const V *__restrict__ pv, const int32_t *__restrict__ pc,
+                                                            int4 d, const X *__restrict__ x, uint32_t lane,
+                                                            uint64_t pol) {
+  return lane_sum_vec<V, X, L1, int32_t>(pv, pc + (uint32_t)d.x, 0, d, x, lane, pol);
 }
 
 // ---- compressed column indices ---------------------------------------------------
@@ -193,87 +257,14 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_fast(const V *__restrict
 // 16-bit offsets from a per-warp base (2 bytes per slot instead of 4); other
 // warps keep 32-bit indices in a compact side array.  cdesc = {base, mode
 // (0 = 16-bit, 1 = 32-bit), offset of the warp in the 32-bit array, 0}.
-__device__ __forceinline__ void ld_stream4(const uint16_t *p, int (&c)[4], int base, uint64_t pol) {
-  unsigned a, b;
-  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.b32 {%0,%1}, [%2], %3;"
-               : "=r"(a), "=r"(b)
-               : "l"(p), "l"(pol));
-  c[0] = base + (int)(a & 0xffffu);
-  c[1] = base + (int)(a >> 16);
-  c[2] = base + (int)(b & 0xffffu);
-  c[3] = base + (int)(b >> 16);
-}
-__device__ __forceinline__ int ld_stream1(const uint16_t *p, int base, uint64_t pol) {
-  unsigned short v;
-  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(v) : "l"(p), "l"(pol));
-  return base + (int)v;
-}
-
-template <typename V, typename X, bool L1, typename C>
-__device__ __forceinline__ typename Tr<V>::Acc lane_sum_fast_cols(const V *__restrict__ pv, const C *__restrict__ cp0,
-                                                                 int base, int4 d, const X *__restrict__ x,
-                                                                 uint32_t lane, uint64_t pol) {
-  typedef typename Tr<V>::Acc Acc;
-  const uint32_t A = (uint32_t)d.y;
-  const size_t o = (size_t)(uint32_t)d.x;
-  const uint32_t units = A >> 2, rem = A & 3u;
-  Acc a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-  const V *vp = pv + o + 4 * lane;
-  const C *cp = cp0 + 4 * lane;
-#pragma unroll 2
-  for (uint32_t u = 0; u < units; u++) {
-    V v[4];
-    int c[4];
-    ld_stream(vp, v, pol);
-    if constexpr (sizeof(C) == 2)
-      ld_stream4(cp, c, base, pol);
-    else
-      ld_stream4(cp, c, pol);
-    a0 = fma_acc(Tr<V>::acc(v[0]), (Acc)Tr<X>::acc(gather<L1>(x, c[0])), a0);
-    a1 = fma_acc(Tr<V>::acc(v[1]), (Acc)Tr<X>::acc(gather<L1>(x, c[1])), a1);
-    a2 = fma_acc(Tr<V>::acc(v[2]), (Acc)Tr<X>::acc(gather<L1>(x, c[2])), a2);
-    a3 = fma_acc(Tr<V>::acc(v[3]), (Acc)Tr<X>::acc(gather<L1>(x, c[3])), a3);
-    vp += 4 * WS;
-    cp += 4 * WS;
-  }
-  Acc tail = Acc(0);
-  const size_t ut = (size_t)units * 4 * WS + lane;
-  for (uint32_t i = 0; i < rem; i++) {
-    int c;
-    if constexpr (sizeof(C) == 2)
-      c = ld_stream1(cp0 + ut + (size_t)i * WS, base, pol);
-    else
-      c = ld_stream1(cp0 + ut + (size_t)i * WS, pol);
-    tail = fma_acc(Tr<V>::acc(ld_stream1(pv + o + ut + (size_t)i * WS, pol)), (Acc)Tr<X>::acc(gather<L1>(x, c)), tail);
-  }
-  a0 += __shfl_xor_sync(0xffffffffu, a0, 8);
-  a1 += __shfl_xor_sync(0xffffffffu, a1, 8);
-  a2 += __shfl_xor_sync(0xffffffffu, a2, 8);
-  a3 += __shfl_xor_sync(0xffffffffu, a3, 8);
-  a0 += __shfl_xor_sync(0xffffffffu, a0, 16);
-  a1 += __shfl_xor_sync(0xffffffffu, a1, 16);
-  a2 += __shfl_xor_sync(0xffffffffu, a2, 16);
-  a3 += __shfl_xor_sync(0xffffffffu, a3, 16);
-  const int src = (int)(lane >> 2);
-  Acc t0 = __shfl_sync(0xffffffffu, a0, src);
-  Acc t1 = __shfl_sync(0xffffffffu, a1, src);
-  Acc t2 = __shfl_sync(0xffffffffu, a2, src);
-  Acc t3 = __shfl_sync(0xffffffffu, a3, src);
-  const uint32_t k = lane & 3u;
-  Acc s = k == 0 ? t0 : k == 1 ? t1 : k == 2 ? t2 : t3;
-  return s + tail;
-}
-
-// Row sums with compressed columns: c16 is indexed by slot, c32 by the warp's
-// compact offset (cdesc.z) plus the slot's position in the warp.
 template <typename V, typename X, bool L1>
 __device__ __forceinline__ typename Tr<V>::Acc lane_sum_compressed(const V *__restrict__ pv,
                                                                   const uint16_t *__restrict__ c16,
                                                                   const int32_t *__restrict__ c32, int4 d,
                                                                   int4 cd, const X *__restrict__ x,
                                                                   uint32_t lane, uint64_t pol) {
-  if (cd.y == 0) return lane_sum_fast_cols<V, X, L1, uint16_t>(pv, c16 + (uint32_t)d.x, cd.x, d, x, lane, pol);
-  return lane_sum_fast_cols<V, X, L1, int32_t>(pv, c32 + (uint32_t)cd.z, 0, d, x, lane, pol);
+  if (cd.y == 0) return lane_sum_vec<V, X, L1, uint16_t>(pv, c16 + (uint32_t)d.x, cd.x, d, x, lane, pol);
+  return lane_sum_vec<V, X, L1, int32_t>(pv, c32 + (uint32_t)cd.z, 0, d, x, lane, pol);
 }
 
 }  // namespace core
