@@ -257,6 +257,50 @@ wk_status wk_cg(wk_engine *e, const double *b, double *x, wk_cg_params *p, void 
 wk_status wk_ir_cg(wk_engine *e64, wk_engine *lo, const double *b, double *x, wk_cg_params *p,
                    void *stream);
 
+/* ---- adjoint (no reference counterpart; differentiable SpMV) ------------- */
+
+typedef struct wk_adjoint wk_adjoint;
+
+/* Builds A^T's WPK layout (kind WK_WPK1 / WK_WPK2 with `threshold`) and
+ * engine on the device from the forward engine `fwd` (WK_F64 or WK_F32):
+ * the CSR entries are stably sorted by column, so no atomics touch values and
+ * results are deterministic.  `fwd` must outlive the adjoint.  When A is
+ * structurally symmetric with sorted rows and kind/threshold equal fwd's,
+ * both layouts coincide and wk_adjoint_run uses one fused pass. */
+wk_status wk_adjoint_create(wk_engine *fwd, int kind, int32_t threshold, void *stream, wk_adjoint **out);
+
+/* New values: vals_csr (nz, CSR order, host or device, fwd's dtype) are
+ * loaded into the forward engine and A^T's engine; vals_csr = NULL re-derives
+ * A^T's values from the forward engine's current values. */
+wk_status wk_adjoint_refresh(wk_adjoint *a, const void *vals_csr, void *stream);
+
+/* Index order of dvals. */
+enum {
+  WK_DVALS_CSR = 0,   /* nz entries, CSR order of the values given to the engine */
+  WK_DVALS_SLOTS = 1  /* allocate_nz entries, the forward layout's padded slot order
+                       * (engine.device_values order; padding slots get 0) */
+};
+
+/* dx = A^T dy (ncols entries; NULL to skip) and dvals = dy[row(k)] x[col(k)]
+ * for every stored entry k (NULL to skip), in `dvals_order`.  x, dy, dx,
+ * dvals are device vectors of fwd's dtype.  WK_DVALS_SLOTS writes the
+ * gradient where the values are stored, with coalesced vector stores (the
+ * fastest form).  Stream-ordered. */
+wk_status wk_adjoint_run(wk_adjoint *a, const void *x, const void *dy, void *dx, void *dvals,
+                         int dvals_order, void *stream);
+
+/* New values in slot order (allocate_nz entries, device or host; padding
+ * ignored), loaded into the forward engine and A^T's engine. */
+wk_status wk_adjoint_refresh_slots(wk_adjoint *a, const void *vals_slots, void *stream);
+
+/* *symmetric = 1 when the fused path is used; tinfo = A^T's layout info. */
+wk_status wk_adjoint_info(const wk_adjoint *a, int *symmetric, wk_layout_info *tinfo);
+
+/* A new reference to A^T's layout (release it with wk_layout_destroy). */
+wk_status wk_adjoint_transposed_layout(const wk_adjoint *a, wk_layout **tl);
+
+wk_status wk_adjoint_destroy(wk_adjoint *a);
+
 /* ---- verification ------------------------------------------------------- */
 
 /* engine::verify(orig, comp) -- warpkernel.hpp:932-943 (host arrays of nrows

@@ -1,0 +1,189 @@
+"""Adjoint of the WPK SpMV: dx = A^T dy and dvals through torch.autograd,
+checked against the host CSR-transpose gradient (oracle) and fp64 central
+finite differences of loss = 0.5 ||A(vals) x - t||^2."""
+import numpy as np
+import pytest
+
+from conftest import random_csr
+from oracle import wk_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def host_grads(rp, cols, vals, x, t):
+    """Reference gradient of 0.5||A x - t||^2 on the host CSR."""
+    y = O.csr_spmv(rp, cols, vals, x)
+    dy = y - t
+    dx = O.csr_spmv_t(rp, cols, vals, dy, len(x))
+    rows = np.repeat(np.arange(len(rp) - 1), np.diff(rp))
+    dvals = dy[rows] * x[cols]
+    return y, dx, dvals
+
+
+def run_autograd(mat, vals, x, t):
+    import torch
+    v = torch.from_numpy(vals).cuda().requires_grad_(True)
+    xx = torch.from_numpy(x).cuda().requires_grad_(True)
+    tt = torch.from_numpy(t).cuda()
+    y = mat.matvec(v, xx)
+    loss = 0.5 * torch.sum((y - tt) ** 2)
+    loss.backward()
+    return y.detach().cpu().numpy(), xx.grad.cpu().numpy(), v.grad.cpu().numpy(), loss.item()
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def test_symmetric_fe_matrix_fused_path_fp64():
+    from warpkernel_gb300.autograd import WPKMatrix
+    rp, cols, vals = O.fe_matrix(3, 6, 6, 6, 3, value_mode=1, seed=4)
+    n = len(rp) - 1
+    rng = np.random.default_rng(4)
+    vals = vals * (1 + 0.1 * rng.standard_normal(len(vals)))  # values no longer symmetric
+    x, t = rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)
+    for kind in (1, 2):
+        import torch
+        mat = WPKMatrix(rp, cols, torch.from_numpy(vals), kind=kind, threshold=27 if kind == 2 else None)
+        assert mat.symmetric
+        y, dx, dv, _ = run_autograd(mat, vals, x, t)
+        y_ref, dx_ref, dv_ref = host_grads(rp, cols, vals, x, t)
+        assert rel(y, y_ref) < 1e-12
+        assert rel(dx, dx_ref) < 1e-12
+        assert rel(dv, dv_ref) < 1e-14
+
+
+def test_general_pattern_transposed_layout_fp64():
+    import torch
+
+    from warpkernel_gb300.autograd import WPKMatrix
+    rng = np.random.default_rng(7)
+    for trial in range(4):
+        n, m = 3000, 2500 + 500 * trial  # rectangular, empty rows and columns
+        rp, cols, vals = random_csr(rng, n, 40, p_empty=0.2, ncols=m, wpk2_safe=False)
+        x, t = rng.uniform(-1, 1, m), rng.uniform(-1, 1, n)
+        mat = WPKMatrix(rp, cols, torch.from_numpy(vals), ncols=m, kind=2, threshold=int(rng.integers(1, 30)))
+        assert not mat.symmetric
+        y, dx, dv, _ = run_autograd(mat, vals, x, t)
+        y_ref, dx_ref, dv_ref = host_grads(rp, cols, vals, x, t)
+        assert rel(y, y_ref) < 1e-12 and rel(dx, dx_ref) < 1e-12 and rel(dv, dv_ref) < 1e-14
+
+
+def test_transposed_layout_matches_oracle_scan_of_the_transpose():
+    import ctypes as C
+
+    import torch
+
+    import warpkernel_gb300 as wk
+    from warpkernel_gb300._lib import check, load
+    from warpkernel_gb300.autograd import WPKMatrix
+    rng = np.random.default_rng(2)
+    n = 2000
+    rp, cols, vals = random_csr(rng, n, 30, p_empty=0.1)
+    mat = WPKMatrix(rp, cols, torch.from_numpy(vals), kind=2, threshold=5)
+    # CSR of A^T on the host, rows ascending
+    order = np.lexsort((np.repeat(np.arange(n), np.diff(rp)), cols))
+    counts = np.bincount(cols, minlength=n)
+    rpT = np.zeros(n + 1, np.int32)
+    rpT[1:] = np.cumsum(counts)
+    h = C.c_void_p()
+    check(load().wk_adjoint_transposed_layout(mat._adj, C.byref(h)))
+    tl = wk.structure2()
+    tl._set(h)
+    with O.OracleLayout(rpT, kind=2, threshold=5) as o:
+        for f in ("row_map", "reorder_rows", "warp_offsets", "max_nz_rows", "threads_per_row", "row_offset_warp"):
+            assert np.array_equal(getattr(tl, f), o.layout.arrays[f]), f
+    assert len(order) == len(cols)
+
+
+def test_central_finite_differences_64_entries():
+    import torch
+
+    from warpkernel_gb300.autograd import WPKMatrix
+    rp, cols, vals = O.fe_matrix(3, 5, 5, 5, 3, value_mode=1, seed=4)
+    n = len(rp) - 1
+    rng = np.random.default_rng(44)
+    x, t = rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)
+    mat = WPKMatrix(rp, cols, torch.from_numpy(vals), kind=2, threshold=81)
+    _, dx, dv, _ = run_autograd(mat, vals, x, t)
+
+    def loss(v, xx):
+        y = O.csr_spmv(rp, cols, v, xx)
+        return 0.5 * float(np.dot(y - t, y - t))
+
+    # the loss is quadratic in each entry, so central differences are exact up
+    # to rounding; a moderate step keeps the rounding small
+    for k in rng.choice(len(vals), 64, replace=False):
+        h = 1e-3
+        vp, vm = vals.copy(), vals.copy()
+        vp[k] += h
+        vm[k] -= h
+        fd = (loss(vp, x) - loss(vm, x)) / (2 * h)
+        assert abs(fd - dv[k]) <= 1e-7 * max(abs(fd), 1e-3), (k, fd, dv[k])
+    for i in rng.choice(n, 64, replace=False):
+        h = 1e-3
+        xp, xm = x.copy(), x.copy()
+        xp[i] += h
+        xm[i] -= h
+        fd = (loss(vals, xp) - loss(vals, xm)) / (2 * h)
+        assert abs(fd - dx[i]) <= 1e-7 * max(abs(fd), 1e-3), (i, fd, dx[i])
+
+
+def test_slot_order_gradient_matches_csr_order():
+    import torch
+
+    from warpkernel_gb300.autograd import WPKMatrix
+    rng = np.random.default_rng(13)
+    cases = [(O.fe_matrix(3, 6, 6, 6, 3, value_mode=1, seed=4), 27), (random_csr(rng, 4000, 30, p_empty=0.2), 7)]
+    for (rp, cols, vals), th in cases:
+        n = len(rp) - 1
+        x, t = rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)
+        m_csr = WPKMatrix(rp, cols, torch.from_numpy(vals), kind=2, threshold=th)
+        _, dx_c, dv_c, _ = run_autograd(m_csr, vals, x, t)
+        m_slot = WPKMatrix(rp, cols, m_csr.to_slots(torch.from_numpy(vals).cuda()), kind=2, threshold=th,
+                           value_order="slots")
+        assert m_slot.symmetric == m_csr.symmetric
+        vs = m_slot.to_slots(torch.from_numpy(vals).cuda()).requires_grad_(True)
+        xx = torch.from_numpy(x).cuda().requires_grad_(True)
+        y = m_slot.matvec(vs, xx)
+        (0.5 * torch.sum((y - torch.from_numpy(t).cuda()) ** 2)).backward()
+        assert rel(xx.grad.cpu().numpy(), dx_c) < 1e-14
+        g = vs.grad
+        assert np.array_equal(m_slot.to_csr(g).cpu().numpy(), dv_c)
+        pad = torch.ones(m_slot.allocate_nz, dtype=torch.bool, device="cuda")
+        pad[m_slot._reorder_rows()] = False
+        assert bool((g[pad] == 0).all())
+        # with 16-bit column storage on the forward engine (fused path reads it too)
+        m_slot.eng.compress_cols()
+        vs.grad = None
+        xx.grad = None
+        y = m_slot.matvec(vs, xx)
+        (0.5 * torch.sum((y - torch.from_numpy(t).cuda()) ** 2)).backward()
+        assert rel(xx.grad.cpu().numpy(), dx_c) < 1e-14
+        assert np.array_equal(m_slot.to_csr(vs.grad).cpu().numpy(), dv_c)
+
+
+def test_fp32_and_value_updates():
+    import torch
+
+    from warpkernel_gb300.autograd import WPKMatrix
+    rp, cols, vals = O.fe_matrix(3, 6, 6, 6, 3, value_mode=1, seed=4)
+    n = len(rp) - 1
+    rng = np.random.default_rng(5)
+    x, t = rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)
+    v32 = torch.from_numpy(vals.astype(np.float32)).cuda().requires_grad_(True)
+    mat = WPKMatrix(rp, cols, v32, kind=2, threshold=81)
+    opt = torch.optim.SGD([v32], lr=1e-3)
+    x32 = torch.from_numpy(x.astype(np.float32)).cuda()
+    t32 = torch.from_numpy(t.astype(np.float32)).cuda()
+    for _ in range(3):  # values change every step: the engines must follow
+        opt.zero_grad()
+        y = mat.matvec(v32, x32)
+        loss = 0.5 * torch.sum((y - t32) ** 2)
+        loss.backward()
+        vh = v32.detach().double().cpu().numpy()
+        y_ref, _, dv_ref = host_grads(rp, cols, vh, x.astype(np.float32).astype(np.float64),
+                                      t.astype(np.float32).astype(np.float64))
+        assert rel(y.detach().double().cpu().numpy(), y_ref) < 1e-5
+        assert rel(v32.grad.double().cpu().numpy(), dv_ref) < 1e-5
+        opt.step()

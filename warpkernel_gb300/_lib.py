@@ -69,6 +69,13 @@ SIGNATURES = {
     "wk_residual_static": (C.c_int, [vp, vp, vp, vp, vp, vp]),
     "wk_cg": (C.c_int, [vp, vp, vp, C.POINTER(CGParams), vp]),
     "wk_ir_cg": (C.c_int, [vp, vp, vp, vp, C.POINTER(CGParams), vp]),
+    "wk_adjoint_create": (C.c_int, [vp, C.c_int, i32, vp, _pvp]),
+    "wk_adjoint_refresh": (C.c_int, [vp, vp, vp]),
+    "wk_adjoint_run": (C.c_int, [vp, vp, vp, vp, vp, C.c_int, vp]),
+    "wk_adjoint_refresh_slots": (C.c_int, [vp, vp, vp]),
+    "wk_adjoint_info": (C.c_int, [vp, _ip, C.POINTER(LayoutInfo)]),
+    "wk_adjoint_transposed_layout": (C.c_int, [vp, _pvp]),
+    "wk_adjoint_destroy": (C.c_int, [vp]),
     "wk_verify": (C.c_int, [vp, vp, vp, _ip, _i64p]),
     "wk_verify_x": (C.c_int, [vp, vp, vp, C.c_int, _ip, _i64p]),
     "wk_fe_size": (C.c_int, [C.c_int] * 5 + [_i64p, _i64p]),

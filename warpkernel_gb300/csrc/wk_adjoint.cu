@@ -1,0 +1,652 @@
+// wk_adjoint.cu -- adjoint of the WPK SpMV: dx = A^T dy through a transposed
+// WPK layout built on the device, and dvals[k] = dy[row(k)] * x[col(k)] over
+// the stored pattern (CSR order).  Deterministic: no atomics on values.
+//
+// Build: the CSR entries of A (recovered from the forward engine through
+// reorder_rows) are stably sorted by column on the device, which gives the
+// CSR of A^T with rows in ascending order and the permutation perm[k'] = k
+// (entry k' of A^T is entry k of A).  A^T's layout and engine then come from
+// the same device scan and process as A's.
+//
+// Structurally symmetric matrices (every finite-element matrix) with sorted
+// rows give A^T the same row offsets and columns as A, so with the same
+// kind/threshold the two layouts coincide slot for slot and the transposed
+// engine's padded values are the mirror values A[c][r] at A's slot (r, c).
+// One fused pass over A's layout then reads mirror value + column per slot,
+// accumulates dx[r] = sum_c A[c][r] dy[c] and writes dvals for the same slot.
+#include <algorithm>
+
+#include "wk_internal.cuh"
+#include "wk_spmv_core.cuh"
+
+struct wk_adjoint {
+  wk_engine *fwd = nullptr;  // not owned: must outlive the adjoint
+  wk_layout *tl = nullptr;   // transposed layout (reference held)
+  wk_engine *te = nullptr;   // transposed engine (owned)
+  wk::DevBuf perm;           // [nz] A^T CSR entry -> A CSR index
+  wk::DevBuf tmp;            // [nz] value staging for refreshes
+  wk::DevBuf xdy;            // [nrows] interleaved (x, dy) of the fused pass
+  bool symmetric = false;
+  int kind = 1;
+  int32_t threshold = 0;
+};
+
+namespace wk {
+namespace {
+
+constexpr int WS = 32;
+
+unsigned grid_for(size_t n, int bs) {
+  size_t g = (n + bs - 1) / bs;
+  if (g < 1) g = 1;
+  if (g > 152u * 64u) g = 152u * 64u;
+  return (unsigned)g;
+}
+
+// CSR-order columns and the identity (sort keys / values), from A's padded arrays.
+__global__ void k_csr_cols(const int32_t *__restrict__ pcols, const uint32_t *__restrict__ reorder_rows, uint32_t nz,
+                           uint32_t *__restrict__ keys, uint32_t *__restrict__ idx) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nz; k += (size_t)gridDim.x * blockDim.x) {
+    keys[k] = (uint32_t)pcols[reorder_rows[k]];
+    idx[k] = (uint32_t)k;
+  }
+}
+
+template <typename E>
+__global__ void k_gather_padded(const E *__restrict__ pv, const uint32_t *__restrict__ reorder_rows, uint32_t nz,
+                                E *__restrict__ out) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nz; k += (size_t)gridDim.x * blockDim.x)
+    out[k] = pv[reorder_rows[k]];
+}
+
+template <typename E>
+__global__ void k_permute(const E *__restrict__ in, const uint32_t *__restrict__ perm, uint32_t nz, E *__restrict__ out) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nz; k += (size_t)gridDim.x * blockDim.x)
+    out[k] = in[perm[k]];
+}
+
+__global__ void k_count(const uint32_t *__restrict__ keys, uint32_t nz, uint32_t *__restrict__ counts) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nz; k += (size_t)gridDim.x * blockDim.x)
+    atomicAdd(&counts[keys[k]], 1u);  // integer counts: order-independent
+}
+
+__global__ void k_row_of(const int32_t *__restrict__ rowptr, uint32_t n, uint32_t *__restrict__ row_of) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (size_t)gridDim.x * blockDim.x)
+    for (int32_t k = rowptr[r]; k < rowptr[r + 1]; k++) row_of[k] = (uint32_t)r;
+}
+
+__global__ void k_count_diff(const uint32_t *__restrict__ a, const uint32_t *__restrict__ b, size_t n,
+                             unsigned *__restrict__ diff) {
+  unsigned c = 0;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    c += a[k] != b[k];
+  c = __reduce_add_sync(0xffffffffu, c);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(diff, c);
+}
+
+// x and dy interleaved, so a slot needs one 8- (fp32) or 16-byte (fp64) gather.
+template <typename T>
+struct Pair;
+template <>
+struct Pair<float> {
+  typedef float2 type;
+};
+template <>
+struct Pair<double> {
+  typedef double2 type;
+};
+
+template <typename T>
+__global__ void k_interleave(const T *__restrict__ x, const T *__restrict__ dy, uint32_t n,
+                             typename Pair<T>::type *__restrict__ xdy) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    typename Pair<T>::type v;
+    v.x = x[i];
+    v.y = dy[i];
+    xdy[i] = v;
+  }
+}
+
+// dvals for the slots of A's layout (general pattern; one warp per layout
+// warp).  SLOTS: dvals indexed by padded slot (padding gets 0), coalesced;
+// otherwise CSR order.
+template <typename T, bool SLOTS>
+__global__ void k_dvals(const int4 *__restrict__ desc, uint32_t W, const int32_t *__restrict__ row_map,
+                        const uint32_t *__restrict__ slen, const int32_t *__restrict__ rowptr, uint32_t nzr,
+                        const int32_t *__restrict__ pc, const T *__restrict__ x, const T *__restrict__ dy,
+                        T *__restrict__ dvals) {
+  const uint32_t lane = threadIdx.x & 31;
+  const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
+  if (w >= W) return;
+  const int4 d = desc[w];
+  const uint32_t T_ = (uint32_t)d.z, A = (uint32_t)d.y, t = lane % T_;
+  const uint32_t p = (uint32_t)d.w + lane / T_;
+  const bool valid = p < nzr;
+  int32_t row = 0;
+  uint32_t len = 0;
+  size_t k0 = 0;
+  T dyr = T(0);
+  if (valid) {
+    row = row_map[p];
+    len = slen[p];
+    k0 = (size_t)rowptr[row];
+    dyr = dy[row];
+  }
+  size_t slot = (size_t)(uint32_t)d.x + lane;
+#pragma unroll 4
+  for (uint32_t i = 0; i < A; i++, slot += WS) {
+    const uint32_t e = i + t * A;
+    const bool real = valid && e < len;
+    if (SLOTS)
+      dvals[slot] = real ? dyr * __ldg(x + __ldcs(pc + slot)) : T(0);
+    else if (real)
+      dvals[k0 + e] = dyr * __ldg(x + __ldcs(pc + slot));
+  }
+}
+
+// Fused adjoint for the coinciding layouts of a structurally symmetric A:
+// dx[r] = sum over row r's slots of mirror value * dy[c], and dvals for each
+// slot.  Reads follow the fast SpMV (lane j streams slots 4j..4j+3 of a
+// 4-step unit: layout lanes 4(j%8)+m at step j/8), with one gather of the
+// interleaved (x, dy) pair per slot.  SLOTS: dvals stored at the same slots
+// with one vector store (padding gets 0).  Otherwise (CSR order) the values of
+// a 16-step chunk are staged in shared memory as [layout lane][step] and
+// written segment by segment -- the entries of one layout lane in one chunk
+// are contiguous in CSR order (e = t*A + step), so a half-warp stores 16
+// consecutive values instead of 32 lanes storing 32 scattered ones.
+constexpr int ADJ_WARPS = 8;
+constexpr int ADJ_CHUNK = 16;
+
+template <typename T, bool SLOTS>
+__global__ void __launch_bounds__(ADJ_WARPS * 32) k_adjoint_sym_vec(
+    const int4 *__restrict__ desc, uint32_t W, const int32_t *__restrict__ row_map, const uint32_t *__restrict__ slen,
+    const int32_t *__restrict__ rowptr, uint32_t nzr, uint32_t nrows, const int32_t *__restrict__ pc,
+    const T *__restrict__ tv, const typename Pair<T>::type *__restrict__ xdy, T *__restrict__ dx,
+    T *__restrict__ dvals) {
+  typedef typename Pair<T>::type P;
+  __shared__ T stage[SLOTS ? 1 : ADJ_WARPS][32][ADJ_CHUNK + 1];
+  __shared__ int2 seg[ADJ_WARPS][32];
+  const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
+  if (w < W) {
+    const int4 d = desc[w];
+    const uint32_t T_ = (uint32_t)d.z, A = (uint32_t)d.y, t = lane % T_;
+    const size_t o = (size_t)(uint32_t)d.x;
+    const uint32_t p = (uint32_t)d.w + lane / T_;
+    const bool valid = p < nzr;
+    int32_t row = 0;
+    int kb = 0, el = 0;
+    T dyr = T(0);
+    if (valid) {
+      row = row_map[p];
+      const int len = (int)slen[p];
+      kb = rowptr[row] + (int)(t * A);
+      el = max(0, min((int)A, len - (int)(t * A)));
+      dyr = xdy[row].y;
+    }
+    if (!SLOTS) seg[wib][lane] = make_int2(kb, el);
+    // dy and the real-entry count of the four layout lanes this lane streams
+    T dyv[4];
+    int elv[4];
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      dyv[m] = __shfl_sync(0xffffffffu, dyr, (int)(4 * (lane & 7) + m));
+      elv[m] = __shfl_sync(0xffffffffu, el, (int)(4 * (lane & 7) + m));
+    }
+    T acc[4] = {T(0), T(0), T(0), T(0)};
+    T tail = T(0);
+    const uint32_t L0 = 4 * (lane & 7), sl = lane >> 3;
+    for (uint32_t i0 = 0; i0 < A; i0 += ADJ_CHUNK) {
+      const uint32_t i1 = min(i0 + (uint32_t)ADJ_CHUNK, A);
+      uint32_t s = i0;
+      for (; s + 4 <= i1; s += 4) {
+        const size_t base = o + (size_t)s * WS + 4 * lane;
+        const int4 c = __ldcs(reinterpret_cast<const int4 *>(pc + base));
+        T v[4];
+        if constexpr (sizeof(T) == 4) {
+          const float4 f = __ldcs(reinterpret_cast<const float4 *>(tv + base));
+          v[0] = f.x; v[1] = f.y; v[2] = f.z; v[3] = f.w;
+        } else {
+          const double2 a0 = __ldcs(reinterpret_cast<const double2 *>(tv + base));
+          const double2 a1 = __ldcs(reinterpret_cast<const double2 *>(tv + base + 2));
+          v[0] = a0.x; v[1] = a0.y; v[2] = a1.x; v[3] = a1.y;
+        }
+        const int cc[4] = {c.x, c.y, c.z, c.w};
+        const uint32_t step = s + sl;
+        T dv[4];
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+          const P g = __ldg(xdy + cc[m]);
+          acc[m] = fma(v[m], g.y, acc[m]);
+          dv[m] = (int)step < elv[m] ? dyv[m] * g.x : T(0);
+        }
+        if constexpr (SLOTS) {
+          if constexpr (sizeof(T) == 4) {
+            *reinterpret_cast<float4 *>(dvals + base) = make_float4(dv[0], dv[1], dv[2], dv[3]);
+          } else {
+            *reinterpret_cast<double2 *>(dvals + base) = make_double2(dv[0], dv[1]);
+            *reinterpret_cast<double2 *>(dvals + base + 2) = make_double2(dv[2], dv[3]);
+          }
+        } else {
+#pragma unroll
+          for (int m = 0; m < 4; m++) stage[wib][L0 + m][step - i0] = dv[m];
+        }
+      }
+      for (; s < i1; s++) {  // the last A % 4 steps: one slot per lane
+        const size_t slot = o + (size_t)s * WS + lane;
+        const int c = __ldcs(pc + slot);
+        const P g = __ldg(xdy + c);
+        tail = fma(__ldcs(tv + slot), g.y, tail);
+        const T dv = (int)s < el ? dyr * g.x : T(0);
+        if (SLOTS)
+          dvals[slot] = dv;
+        else
+          stage[SLOTS ? 0 : wib][lane][s - i0] = dv;
+      }
+      if constexpr (!SLOTS) {
+        __syncwarp();
+        const uint32_t nst = i1 - i0, jj = lane & 15;
+#pragma unroll 4
+        for (uint32_t sg = 0; sg < 32; sg += 2) {
+          const uint32_t sgm = sg + (lane >> 4);
+          const int2 si = seg[wib][sgm];
+          const uint32_t e = i0 + jj;
+          if (jj < nst && (int)e < si.y) dvals[(size_t)si.x + e] = stage[wib][sgm][jj];
+        }
+        __syncwarp();
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      acc[m] += __shfl_xor_sync(0xffffffffu, acc[m], 8);
+      acc[m] += __shfl_xor_sync(0xffffffffu, acc[m], 16);
+    }
+    T s0 = T(0);
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      const T tt = __shfl_sync(0xffffffffu, acc[m], (int)(lane >> 2));
+      if ((lane & 3) == (uint32_t)m) s0 = tt;
+    }
+    T total = s0 + tail;
+    for (uint32_t k = 1; k < T_; k <<= 1) total += __shfl_down_sync(0xffffffffu, total, k);
+    if (valid && (lane & (T_ - 1)) == 0) dx[row] = total;
+  }
+  for (size_t q = (size_t)nzr + (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < nrows;
+       q += (size_t)gridDim.x * blockDim.x)
+    dx[row_map[q]] = T(0);
+}
+
+// Fused adjoint, slot order: the streaming pattern of the fast SpMV with S
+// slots per lane (S = 4 for fp64, 8 for fp32), 256-bit loads of mirror
+// values and columns, and one 256-bit store of the S gradients per lane.
+__device__ __forceinline__ void st_words(void *p, const uint32_t (&w)[8]) {
+  asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "r"(w[0]), "r"(w[1]), "r"(w[2]),
+               "r"(w[3]), "r"(w[4]), "r"(w[5]), "r"(w[6]), "r"(w[7])
+               : "memory");
+}
+__device__ __forceinline__ void put_word(uint32_t *w, int k, float v) { w[k] = __float_as_uint(v); }
+__device__ __forceinline__ void put_word(uint32_t *w, int k, double v) {
+  w[2 * k] = (uint32_t)__double2loint(v);
+  w[2 * k + 1] = (uint32_t)__double2hiint(v);
+}
+
+// One layout warp of the slot-order adjoint; columns as int32 (C = int32_t)
+// or as 16-bit offsets from `base` (C = uint16_t).  Returns layout lane
+// `lane`'s sum of mirror value * dy[c].
+template <typename T, typename C>
+__device__ __forceinline__ T adjoint_warp_slots(const int4 d, const C *__restrict__ cp0, int base,
+                                                const T *__restrict__ tv, const typename Pair<T>::type *__restrict__ xdy,
+                                                T *__restrict__ dvals, const T (&dyv)[core::SlotsPerLane<T>::value],
+                                                const int (&elv)[core::SlotsPerLane<T>::value], T dyr, int el,
+                                                uint32_t lane, uint64_t pol) {
+  using namespace core;
+  typedef typename Pair<T>::type P;
+  constexpr int S = SlotsPerLane<T>::value, R = 32 / S;
+  const uint32_t A = (uint32_t)d.y;
+  const size_t o = (size_t)(uint32_t)d.x;
+  T acc[S];
+#pragma unroll
+  for (int m = 0; m < S; m++) acc[m] = T(0);
+  const uint32_t units = A / S, rem = A % S, sl = lane / R;
+  const T *vp = tv + o + S * lane;
+  const C *cp = cp0 + S * lane;
+  T *dp = dvals + o + S * lane;
+#pragma unroll 2
+  for (uint32_t u = 0; u < units; u++) {
+    uint32_t wv[S * sizeof(T) / 4], wc[S * sizeof(C) / 4], wd[8];
+    ld_words(vp, wv, pol);
+    ld_words(cp, wc, pol);
+    const int step = (int)(u * S + sl);
+#pragma unroll
+    for (int m = 0; m < S; m++) {
+      const P g = __ldg(xdy + word_col<C>(wc, m, base));
+      acc[m] = fma(word_val<T>(wv, m), g.y, acc[m]);
+      put_word(wd, m, step < elv[m] ? dyv[m] * g.x : T(0));
+    }
+    st_words(dp, wd);
+    vp += S * WS;
+    cp += S * WS;
+    dp += S * WS;
+  }
+  T tail = T(0);
+  const size_t ut = (size_t)units * S * WS + lane;
+  for (uint32_t i = 0; i < rem; i++) {
+    const size_t k = ut + (size_t)i * WS;
+    const P g = __ldg(xdy + ld_col1(cp0 + k, base, pol));
+    tail = fma(__ldcs(tv + o + k), g.y, tail);
+    dvals[o + k] = (int)(units * S + i) < el ? dyr * g.x : T(0);
+  }
+#pragma unroll
+  for (int mm = R; mm < 32; mm <<= 1) {
+#pragma unroll
+    for (int m = 0; m < S; m++) acc[m] += __shfl_xor_sync(0xffffffffu, acc[m], mm);
+  }
+  T s0 = T(0);
+#pragma unroll
+  for (int m = 0; m < S; m++) {
+    const T tt = __shfl_sync(0xffffffffu, acc[m], (int)(lane / S));
+    if (lane % S == (uint32_t)m) s0 = tt;
+  }
+  return s0 + tail;
+}
+
+template <typename T, bool COMP>
+__global__ void __launch_bounds__(256) k_adjoint_sym_slots(
+    const int4 *__restrict__ desc, uint32_t W, const int32_t *__restrict__ row_map, const uint32_t *__restrict__ slen,
+    uint32_t nzr, uint32_t nrows, const int32_t *__restrict__ pc, const uint16_t *__restrict__ c16,
+    const int32_t *__restrict__ c32, const int4 *__restrict__ cdesc, const T *__restrict__ tv,
+    const typename Pair<T>::type *__restrict__ xdy, T *__restrict__ dx, T *__restrict__ dvals) {
+  using namespace core;
+  constexpr int S = SlotsPerLane<T>::value, R = 32 / S;
+  const uint32_t lane = threadIdx.x & 31;
+  const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
+  if (w < W) {
+    const uint64_t pol = policy_evict_first();
+    const int4 d = desc[w];
+    const uint32_t T_ = (uint32_t)d.z, A = (uint32_t)d.y, t = lane % T_;
+    const uint32_t p = (uint32_t)d.w + lane / T_;
+    const bool valid = p < nzr;
+    int32_t row = 0;
+    int el = 0;
+    T dyr = T(0);
+    if (valid) {
+      row = row_map[p];
+      el = max(0, min((int)A, (int)slen[p] - (int)(t * A)));
+      dyr = xdy[row].y;
+    }
+    T dyv[S];
+    int elv[S];
+#pragma unroll
+    for (int m = 0; m < S; m++) {
+      dyv[m] = __shfl_sync(0xffffffffu, dyr, (int)(S * (lane % R) + m));
+      elv[m] = __shfl_sync(0xffffffffu, el, (int)(S * (lane % R) + m));
+    }
+    T total;
+    if constexpr (COMP) {
+      const int4 cd = cdesc[w];
+      if (cd.y == 0)
+        total = adjoint_warp_slots<T, uint16_t>(d, c16 + (uint32_t)d.x, cd.x, tv, xdy, dvals, dyv, elv, dyr, el, lane,
+                                                pol);
+      else
+        total = adjoint_warp_slots<T, int32_t>(d, c32 + (uint32_t)cd.z, 0, tv, xdy, dvals, dyv, elv, dyr, el, lane,
+                                               pol);
+    } else {
+      total = adjoint_warp_slots<T, int32_t>(d, pc + (uint32_t)d.x, 0, tv, xdy, dvals, dyv, elv, dyr, el, lane, pol);
+    }
+    for (uint32_t k = 1; k < T_; k <<= 1) total += __shfl_down_sync(0xffffffffu, total, k);
+    if (valid && (lane & (T_ - 1)) == 0) dx[row] = total;
+  }
+  for (size_t q = (size_t)nzr + (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < nrows;
+       q += (size_t)gridDim.x * blockDim.x)
+    dx[row_map[q]] = T(0);
+}
+
+wk_status refresh_transposed(wk_adjoint *a, const void *vals_csr, cudaStream_t st) {
+  const wk_engine *f = a->fwd;
+  const uint32_t nz = f->layout->info.nz;
+  const size_t eb = dtype_size(f->dtype);
+  const void *src = vals_csr;
+  if (!src) {  // from the forward engine's padded values
+    if (eb == 8)
+      k_gather_padded<unsigned long long><<<grid_for(nz, 256), 256, 0, st>>>(
+          f->vals.as<unsigned long long>(), f->layout->d.reorder_rows, nz, a->tmp.as<unsigned long long>());
+    else
+      k_gather_padded<uint32_t><<<grid_for(nz, 256), 256, 0, st>>>(f->vals.as<uint32_t>(), f->layout->d.reorder_rows,
+                                                                   nz, a->tmp.as<uint32_t>());
+    WK_CHECK_LAUNCH();
+    src = a->tmp.p;
+  }
+  // tmp2 = vals[perm]: reuse the transposed engine's scratch as the CSR-order staging
+  DevBuf stage;
+  WK_TRY(stage.alloc((size_t)nz * eb));
+  if (eb == 8)
+    k_permute<unsigned long long><<<grid_for(nz, 256), 256, 0, st>>>((const unsigned long long *)src,
+                                                                     a->perm.as<uint32_t>(), nz,
+                                                                     stage.as<unsigned long long>());
+  else
+    k_permute<uint32_t><<<grid_for(nz, 256), 256, 0, st>>>((const uint32_t *)src, a->perm.as<uint32_t>(), nz,
+                                                           stage.as<uint32_t>());
+  WK_CHECK_LAUNCH();
+  WK_TRY(launch_process(a->tl, stage.p, (int)eb, nullptr, a->te->vals.p, nullptr, false, st));
+  WK_CUDA(cudaStreamSynchronize(st));
+  return WK_OK;
+}
+
+}  // namespace
+}  // namespace wk
+
+using namespace wk;
+
+extern "C" wk_status wk_adjoint_create(wk_engine *fwd, int kind, int32_t threshold, void *stream, wk_adjoint **out) {
+  if (!out) return set_error(WK_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  if (!fwd) return set_error(WK_ERR_INVALID, "engine is NULL");
+  if (fwd->dtype != WK_F64 && fwd->dtype != WK_F32)
+    return set_error(WK_ERR_INVALID, "the adjoint supports WK_F64 and WK_F32 engines");
+  if (kind != WK_WPK1 && kind != WK_WPK2) return set_error(WK_ERR_INVALID, "kind must be WK_WPK1 or WK_WPK2");
+  cudaStream_t st = (cudaStream_t)stream;
+  const wk_layout *L = fwd->layout;
+  const uint32_t n = L->info.nrows, m = fwd->ncols, nz = L->info.nz;
+  if (m > 0x7fffffffu) return set_error(WK_ERR_INVALID, "ncols too large");
+  const size_t eb = dtype_size(fwd->dtype);
+  wk_adjoint *a = new (std::nothrow) wk_adjoint();
+  if (!a) return set_error(WK_ERR_ALLOC, "host allocation failed");
+  a->fwd = fwd;
+  a->kind = kind;
+  a->threshold = threshold;
+  auto fail = [&](wk_status s) {
+    if (a->te) wk_engine_destroy(a->te);
+    if (a->tl) wk_layout_destroy(a->tl);
+    delete a;
+    return s;
+  };
+  DevBuf k0, k1, v0, v1, counts, rowptrT, valsc, colsT, rowof, diff, csrcols;
+  wk_status s = WK_OK;
+  if (s == WK_OK) s = k0.alloc((size_t)nz * 4);
+  if (s == WK_OK) s = k1.alloc((size_t)nz * 4);
+  if (s == WK_OK) s = v0.alloc((size_t)nz * 4);
+  if (s == WK_OK) s = v1.alloc((size_t)nz * 4);
+  if (s == WK_OK) s = csrcols.alloc((size_t)nz * 4);
+  if (s == WK_OK) s = counts.alloc(((size_t)m + 1) * 4);
+  if (s == WK_OK) s = rowptrT.alloc(((size_t)m + 1) * 4);
+  if (s == WK_OK) s = a->tmp.alloc((size_t)nz * eb);
+  if (s == WK_OK) s = colsT.alloc((size_t)nz * 4);
+  if (s == WK_OK) s = rowof.alloc((size_t)nz * 4);
+  if (s == WK_OK) s = diff.alloc(16);
+  if (s != WK_OK) return fail(s);
+  // CSR columns of A, then a stable sort by column: perm and A^T's columns
+  k_csr_cols<<<grid_for(nz, 256), 256, 0, st>>>(fwd->cols.as<int32_t>(), L->d.reorder_rows, nz, k0.as<uint32_t>(),
+                                                v0.as<uint32_t>());
+  if (cudaMemcpyAsync(csrcols.p, k0.p, (size_t)nz * 4, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+    return fail(set_error(WK_ERR_CUDA, "copy failed"));
+  if (cudaMemsetAsync(counts.p, 0, ((size_t)m + 1) * 4, st) != cudaSuccess)
+    return fail(set_error(WK_ERR_CUDA, "memset failed"));
+  k_count<<<grid_for(nz, 256), 256, 0, st>>>(k0.as<uint32_t>(), nz, counts.as<uint32_t>());
+  if (cudaGetLastError() != cudaSuccess) return fail(set_error(WK_ERR_CUDA, "kernel launch failed"));
+  s = scan_u32(counts.as<uint32_t>(), rowptrT.as<uint32_t>(), (size_t)m + 1, nullptr, st);
+  if (s != WK_OK) return fail(s);
+  int bits = 0;
+  while (bits < 32 && (((uint64_t)m > 0 ? (uint64_t)m - 1 : 0) >> bits)) bits++;
+  int cur = 0;
+  s = radix_sort_pairs(k0.as<uint32_t>(), k1.as<uint32_t>(), v0.as<uint32_t>(), v1.as<uint32_t>(), nz, bits, st, &cur);
+  if (s != WK_OK) return fail(s);
+  s = a->perm.alloc((size_t)nz * 4);
+  if (s != WK_OK) return fail(s);
+  const uint32_t *perm = cur ? v1.as<uint32_t>() : v0.as<uint32_t>();
+  if (cudaMemcpyAsync(a->perm.p, perm, (size_t)nz * 4, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+    return fail(set_error(WK_ERR_CUDA, "copy failed"));
+  k_row_of<<<grid_for(n, 256), 256, 0, st>>>(L->d.rowptr, n, rowof.as<uint32_t>());
+  k_permute<uint32_t><<<grid_for(nz, 256), 256, 0, st>>>(rowof.as<uint32_t>(), a->perm.as<uint32_t>(), nz,
+                                                         colsT.as<uint32_t>());
+  if (cudaGetLastError() != cudaSuccess) return fail(set_error(WK_ERR_CUDA, "kernel launch failed"));
+  // A^T's layout and engine (values in A^T's CSR order = A's values permuted)
+  s = make_layout(rowptrT.as<int32_t>(), m, nz, kind, threshold, st, &a->tl);
+  if (s != WK_OK) return fail(s);
+  if (eb == 8)
+    k_gather_padded<unsigned long long><<<grid_for(nz, 256), 256, 0, st>>>(
+        fwd->vals.as<unsigned long long>(), L->d.reorder_rows, nz, a->tmp.as<unsigned long long>());
+  else
+    k_gather_padded<uint32_t><<<grid_for(nz, 256), 256, 0, st>>>(fwd->vals.as<uint32_t>(), L->d.reorder_rows, nz,
+                                                                 a->tmp.as<uint32_t>());
+  s = valsc.alloc((size_t)nz * eb);
+  if (s != WK_OK) return fail(s);
+  if (eb == 8)
+    k_permute<unsigned long long><<<grid_for(nz, 256), 256, 0, st>>>(a->tmp.as<unsigned long long>(),
+                                                                     a->perm.as<uint32_t>(), nz,
+                                                                     valsc.as<unsigned long long>());
+  else
+    k_permute<uint32_t><<<grid_for(nz, 256), 256, 0, st>>>(a->tmp.as<uint32_t>(), a->perm.as<uint32_t>(), nz,
+                                                           valsc.as<uint32_t>());
+  s = make_engine(a->tl, fwd->dtype, valsc.p, colsT.as<int32_t>(), n, st, &a->te);
+  if (s != WK_OK) return fail(s);
+  // structurally symmetric with sorted rows: same row offsets and columns
+  if (m == n && kind == L->info.kind && (kind == WK_WPK1 || (uint32_t)threshold == L->info.nmax_per_thread)) {
+    if (cudaMemsetAsync(diff.p, 0, 4, st) != cudaSuccess) return fail(set_error(WK_ERR_CUDA, "memset failed"));
+    k_count_diff<<<grid_for((size_t)n + 1, 256), 256, 0, st>>>(rowptrT.as<uint32_t>(), (const uint32_t *)L->d.rowptr,
+                                                               (size_t)n + 1, diff.as<unsigned>());
+    k_count_diff<<<grid_for(nz, 256), 256, 0, st>>>(colsT.as<uint32_t>(), csrcols.as<uint32_t>(), nz,
+                                                    diff.as<unsigned>());
+    unsigned h = 1;
+    if (cudaMemcpyAsync(&h, diff.p, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return fail(set_error(WK_ERR_CUDA, "symmetry check failed"));
+    a->symmetric = h == 0;
+  }
+  if (cudaStreamSynchronize(st) != cudaSuccess) return fail(set_error(WK_ERR_CUDA, "adjoint build failed"));
+  *out = a;
+  return WK_OK;
+}
+
+extern "C" wk_status wk_adjoint_refresh(wk_adjoint *a, const void *vals_csr, void *stream) {
+  if (!a) return set_error(WK_ERR_INVALID, "adjoint is NULL");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (vals_csr) {
+    WK_TRY(wk_engine_set_values(a->fwd, vals_csr, stream));
+    DevView v;
+    WK_TRY(v.from(vals_csr, (size_t)a->fwd->layout->info.nz * dtype_size(a->fwd->dtype), st));
+    return refresh_transposed(a, v.dptr, st);
+  }
+  return refresh_transposed(a, nullptr, st);
+}
+
+extern "C" wk_status wk_adjoint_run(wk_adjoint *a, const void *x, const void *dy, void *dx, void *dvals,
+                                   int dvals_order, void *stream) {
+  if (!a || !dy) return set_error(WK_ERR_INVALID, "NULL argument");
+  if (dvals && !x) return set_error(WK_ERR_INVALID, "dvals needs x");
+  if (dvals_order != WK_DVALS_CSR && dvals_order != WK_DVALS_SLOTS)
+    return set_error(WK_ERR_INVALID, "unknown dvals order %d", dvals_order);
+  cudaStream_t st = (cudaStream_t)stream;
+  const wk_engine *f = a->fwd;
+  const wk_layout *L = f->layout;
+  const uint32_t W = L->info.nwarps, n = L->info.nrows;
+  const bool f64 = f->dtype == WK_F64;
+  const bool slots = dvals_order == WK_DVALS_SLOTS;
+  if (a->symmetric && dx && dvals) {
+    const size_t pb = (size_t)n * (f64 ? 16 : 8);
+    if (a->xdy.bytes < pb) WK_TRY(a->xdy.alloc(pb));
+    const unsigned gi = grid_for(n, 256);
+    const unsigned gv = (unsigned)std::max<size_t>(1, ((size_t)W + ADJ_WARPS - 1) / ADJ_WARPS);
+#define WK_ADJ(T, S)                                                                                                 \
+  k_adjoint_sym_vec<T, S><<<gv, ADJ_WARPS * 32, 0, st>>>(                                                            \
+      L->d.warp_desc, W, L->d.row_map, L->d.slen, L->d.rowptr, L->info.nznrows, n, f->cols.as<int32_t>(),            \
+      a->te->vals.as<T>(), a->xdy.as<typename Pair<T>::type>(), (T *)dx, (T *)dvals)
+#define WK_ADJ_SLOTS(T)                                                                                             \
+  do {                                                                                                              \
+    const unsigned gs = (unsigned)std::max<size_t>(1, ((size_t)W + 7) / 8);                                        \
+    if (f->compressed)                                                                                              \
+      k_adjoint_sym_slots<T, true><<<gs, 256, 0, st>>>(                                                             \
+          L->d.warp_desc, W, L->d.row_map, L->d.slen, L->info.nznrows, n, f->cols.as<int32_t>(),                    \
+          f->c16.as<uint16_t>(), f->c32.as<int32_t>(), f->cdesc.as<int4>(), a->te->vals.as<T>(),                    \
+          a->xdy.as<typename Pair<T>::type>(), (T *)dx, (T *)dvals);                                                \
+    else                                                                                                            \
+      k_adjoint_sym_slots<T, false><<<gs, 256, 0, st>>>(                                                            \
+          L->d.warp_desc, W, L->d.row_map, L->d.slen, L->info.nznrows, n, f->cols.as<int32_t>(), nullptr, nullptr,  \
+          nullptr, a->te->vals.as<T>(), a->xdy.as<typename Pair<T>::type>(), (T *)dx, (T *)dvals);                 \
+  } while (0)
+    if (slots && ((uintptr_t)dvals & 31u))
+      return set_error(WK_ERR_INVALID, "slot-order dvals must be 32-byte aligned");
+    if (f64) {
+      k_interleave<double><<<gi, 256, 0, st>>>((const double *)x, (const double *)dy, n, a->xdy.as<double2>());
+      if (slots) WK_ADJ_SLOTS(double); else WK_ADJ(double, false);
+    } else {
+      k_interleave<float><<<gi, 256, 0, st>>>((const float *)x, (const float *)dy, n, a->xdy.as<float2>());
+      if (slots) WK_ADJ_SLOTS(float); else WK_ADJ(float, false);
+    }
+#undef WK_ADJ
+#undef WK_ADJ_SLOTS
+    WK_CHECK_LAUNCH();
+    return WK_OK;
+  }
+  if (dx) {
+    const size_t yb = (size_t)a->te->layout->info.nrows * dtype_size(f->dtype);
+    if (a->te->layout->info.nznrows < a->te->layout->info.nrows) WK_CUDA(cudaMemsetAsync(dx, 0, yb, st));
+    RunArgs ra{a->te, 0, 0, 1, WK_ORDER_FAST, true, dy, dx, st};
+    WK_TRY(launch_spmv(ra));
+  }
+  if (dvals && W) {
+    const unsigned g = (unsigned)std::max<size_t>(1, ((size_t)W * WS + 255) / 256);
+#define WK_DV(T, S)                                                                                                    \
+  k_dvals<T, S><<<g, 256, 0, st>>>(L->d.warp_desc, W, L->d.row_map, L->d.slen, L->d.rowptr, L->info.nznrows,           \
+                                   f->cols.as<int32_t>(), (const T *)x, (const T *)dy, (T *)dvals)
+    if (f64) {
+      if (slots) WK_DV(double, true); else WK_DV(double, false);
+    } else {
+      if (slots) WK_DV(float, true); else WK_DV(float, false);
+    }
+#undef WK_DV
+    WK_CHECK_LAUNCH();
+  }
+  return WK_OK;
+}
+
+// Values in slot order (allocate_nz, padding ignored): copied into the forward
+// engine, then A^T's values are re-derived from it.
+extern "C" wk_status wk_adjoint_refresh_slots(wk_adjoint *a, const void *vals_slots, void *stream) {
+  if (!a || !vals_slots) return set_error(WK_ERR_INVALID, "NULL argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t bytes = (size_t)a->fwd->layout->info.allocate_nz * dtype_size(a->fwd->dtype);
+  if (bytes) WK_CUDA(cudaMemcpyAsync(a->fwd->vals.p, vals_slots, bytes, cudaMemcpyDefault, st));
+  return refresh_transposed(a, nullptr, st);
+}
+
+extern "C" wk_status wk_adjoint_info(const wk_adjoint *a, int *symmetric, wk_layout_info *tinfo) {
+  if (!a) return set_error(WK_ERR_INVALID, "adjoint is NULL");
+  if (symmetric) *symmetric = a->symmetric ? 1 : 0;
+  if (tinfo) *tinfo = a->tl->info;
+  return WK_OK;
+}
+
+extern "C" wk_status wk_adjoint_transposed_layout(const wk_adjoint *a, wk_layout **tl) {
+  if (!a || !tl) return set_error(WK_ERR_INVALID, "NULL argument");
+  a->tl->refs.fetch_add(1);
+  *tl = a->tl;
+  return WK_OK;
+}
+
+extern "C" wk_status wk_adjoint_destroy(wk_adjoint *a) {
+  if (!a) return WK_OK;
+  if (a->te) wk_engine_destroy(a->te);
+  if (a->tl) wk_layout_destroy(a->tl);
+  delete a;
+  return WK_OK;
+}

@@ -128,6 +128,13 @@ wk_status scan_common(const int32_t *rowptr, uint32_t nrows, uint32_t nz, int ki
 
 }  // namespace
 
+namespace wk {
+wk_status make_layout(const int32_t *d_rowptr, uint32_t nrows, uint32_t nz, int kind, int32_t threshold,
+                      cudaStream_t stream, wk_layout **out) {
+  return scan_common(d_rowptr, nrows, nz, kind, threshold, stream, out);
+}
+}  // namespace wk
+
 extern "C" {
 
 size_t wk_last_error(char *buf, size_t cap) {
@@ -475,3 +482,10 @@ wk_status wk_convert(const void *src, int sdt, void *dst, int ddt, int64_t n, vo
 }
 
 }  // extern "C"
+
+namespace wk {
+wk_status make_engine(wk_layout *l, int dtype, const void *d_vals, const int32_t *d_cols, uint32_t ncols,
+                      cudaStream_t stream, wk_engine **out) {
+  return wk_engine_create(l, dtype, d_vals, d_cols, ncols, stream, out);
+}
+}  // namespace wk

@@ -150,6 +150,19 @@ wk_status launch_check_cols(const int32_t *cols, size_t n, uint32_t ncols, int *
 // Synchronises `stream`.
 wk_status scan_u64(const unsigned long long *in, unsigned long long *out, size_t n,
                    unsigned long long *d_total, cudaStream_t stream);
+wk_status scan_u32(const uint32_t *in, uint32_t *out, size_t n, uint32_t *d_total, cudaStream_t stream);
+// Stable LSD radix sort of n (key, value) pairs by the low `bits` key bits;
+// input in buffers 0, *out = which buffer pair holds the result.
+wk_status radix_sort_pairs(uint32_t *k0, uint32_t *k1, uint32_t *v0, uint32_t *v1, uint32_t n, int bits,
+                           cudaStream_t stream, int *out);
+// Allocates a layout and builds it on the device from a device copy of the
+// CSR row offsets (the layout keeps its own copy).
+wk_status make_layout(const int32_t *d_rowptr, uint32_t nrows, uint32_t nz, int kind, int32_t threshold,
+                      cudaStream_t stream, wk_layout **out);
+// Allocates an engine over layout l (takes a layout reference) from device
+// CSR-ordered values (elem bytes 8/4/2) and column indices.
+wk_status make_engine(wk_layout *l, int dtype, const void *d_vals, const int32_t *d_cols, uint32_t ncols,
+                      cudaStream_t stream, wk_engine **out);
 // Builds / refreshes the engine's 16-bit column storage from its int32 columns.
 wk_status build_compressed_cols(wk_engine *e, cudaStream_t stream, uint32_t *wide_warps);
 

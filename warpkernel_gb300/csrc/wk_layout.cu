@@ -417,6 +417,35 @@ unsigned grid_for(size_t n, int bs) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
+// Stable sort of n (key, value) pairs by the low `bits` bits of the key;
+// buffers 0 hold the input, *out = index (0/1) of the buffers with the result.
+wk_status radix_sort_pairs(uint32_t *k0, uint32_t *k1, uint32_t *v0, uint32_t *v1, uint32_t n, int bits,
+                           cudaStream_t st, int *out) {
+  uint32_t *kb[2] = {k0, k1}, *vb[2] = {v0, v1};
+  const uint32_t ntiles = (n + RS_TILE - 1) / RS_TILE;
+  int cur = 0;
+  if (n > 0 && bits > 0) {
+    DevBuf hist;
+    WK_TRY(hist.alloc((size_t)256 * ntiles * 4));
+    const unsigned nblk = (ntiles + RS_WARPS - 1) / RS_WARPS;
+    for (int shift = 0; shift < bits; shift += 8) {
+      k_radix_up<<<nblk, RS_WARPS * 32, 0, st>>>(kb[cur], n, shift, hist.as<uint32_t>(), ntiles);
+      WK_CHECK_LAUNCH();
+      WK_TRY(exclusive_scan<uint32_t>(hist.as<uint32_t>(), hist.as<uint32_t>(), (size_t)256 * ntiles, nullptr, st));
+      k_radix_down<<<nblk, RS_WARPS * 32, 0, st>>>(kb[cur], vb[cur], kb[cur ^ 1], vb[cur ^ 1], n, shift,
+                                                   hist.as<uint32_t>(), ntiles);
+      WK_CHECK_LAUNCH();
+      cur ^= 1;
+    }
+  }
+  *out = cur;
+  return WK_OK;
+}
+
+wk_status scan_u32(const uint32_t *in, uint32_t *out, size_t n, uint32_t *d_total, cudaStream_t st) {
+  return exclusive_scan<uint32_t>(in, out, n, d_total, st);
+}
+
 wk_status build_layout(wk_layout *l, const int32_t *d_rowptr, int kind, int32_t threshold,
                        cudaStream_t st) {
   const uint32_t n = l->info.nrows, nz = l->info.nz;
@@ -452,25 +481,9 @@ wk_status build_layout(wk_layout *l, const int32_t *d_rowptr, int kind, int32_t 
   WK_CHECK_LAUNCH();
   int bits = 0;
   while (bits < 32 && (maxlen >> bits)) bits++;
-  const uint32_t ntiles = (n + RS_TILE - 1) / RS_TILE;
   int cur = 0;
-  if (n > 0 && bits > 0) {
-    DevBuf hist;
-    WK_TRY(hist.alloc((size_t)256 * ntiles * 4));
-    const unsigned nblk = (ntiles + RS_WARPS - 1) / RS_WARPS;
-    for (int shift = 0; shift < bits; shift += 8) {
-      k_radix_up<<<nblk, RS_WARPS * 32, 0, st>>>(kb[cur].as<uint32_t>(), n, shift, hist.as<uint32_t>(),
-                                                 ntiles);
-      WK_CHECK_LAUNCH();
-      WK_TRY(exclusive_scan<uint32_t>(hist.as<uint32_t>(), hist.as<uint32_t>(), (size_t)256 * ntiles,
-                                      nullptr, st));
-      k_radix_down<<<nblk, RS_WARPS * 32, 0, st>>>(kb[cur].as<uint32_t>(), vb[cur].as<uint32_t>(),
-                                                   kb[cur ^ 1].as<uint32_t>(), vb[cur ^ 1].as<uint32_t>(),
-                                                   n, shift, hist.as<uint32_t>(), ntiles);
-      WK_CHECK_LAUNCH();
-      cur ^= 1;
-    }
-  }
+  WK_TRY(radix_sort_pairs(kb[0].as<uint32_t>(), kb[1].as<uint32_t>(), vb[0].as<uint32_t>(), vb[1].as<uint32_t>(), n,
+                          bits, st, &cur));
   LayoutDev &d = l->d;
   WK_TRY(l->bufs[0].alloc((size_t)n * 4));
   WK_TRY(l->bufs[1].alloc((size_t)n * 4));
