@@ -79,7 +79,7 @@ class Clocks:
     def __enter__(self):
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                       "--format=csv,noheader,nounits", "-lms", "50"],
                                       stdout=self.f, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.p = None
@@ -245,10 +245,158 @@ def run_ours(args):
                                          f"OpenMP static rows), median {med * 1e3:.2f} ms"}
         nrm = float(np.linalg.norm(y_cpu))
         out["rel_err_vs_host_csr"] = float(np.linalg.norm(y_host - y_cpu) / nrm) if nrm else 0.0
+    del eng, k, rowptr, cols, vals, x, y, xh, yh
+    torch.cuda.empty_cache()
+    if rank == 0 and not args.no_suites:
+        out["suites"] = run_suites(args)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
     return out, rank
+
+
+# ---- the other rows of the benchmark table ---------------------------------------
+
+def _event_ms(fn, reps, warm=3):
+    import torch
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def suite_mixed_and_cg(reps):
+    """hex 96^3 (3 dof, seed 2): fp64 vs FP32 / BF16-stored SpMV with FP32
+    accumulation (error vs the fp64 host CSR product), then fp64 CG vs
+    iterative-refinement CG to 1e-10 with b = A x*."""
+    import numpy as np
+    import torch
+
+    import warpkernel_gb300 as wk
+    from oracle import wk_oracle as O
+    from warpkernel_gb300 import fe
+    rp, cols, vals = fe.fe_matrix(3, 96, 96, 96, 3, 1, 2)
+    n, nnz = rp.numel() - 1, cols.numel()
+    x = fe.uniform_vec(2, 0, n)
+    y_ref = O.csr_spmv(rp.cpu().numpy(), cols.cpu().numpy(), vals.cpu().numpy(), x.cpu().numpy())
+    k = wk.structure2().scan(nnz, n, None, rp, None, 81)
+    res = {"workload": "hex96_3dof seed 2", "nrows": n, "nnz": nnz, "paths": {}}
+    e64 = wk.engine(k, vals, cols)
+    y64 = torch.zeros(n, dtype=torch.float64, device="cuda")
+    ms64 = _event_ms(lambda: e64.run(0, 128, x, y64, timed=False), reps)
+    base = nnz / ms64
+    res["paths"]["f64"] = {"ms": round(ms64, 4), "gnnz_s": round(nnz / ms64 / 1e6, 1), "speedup": 1.0,
+                           "gbs": round((12 * nnz + 20 * n) / ms64 / 1e6, 1),
+                           "rel_err": float(np.linalg.norm(y64.cpu().numpy() - y_ref) / np.linalg.norm(y_ref))}
+    engines = {}
+    for name, tdt, dt, vb in (("f32", torch.float32, "f32", 4), ("bf16", torch.bfloat16, "bf16", 2)):
+        e = wk.engine(k, fe.convert(vals, tdt), cols, dtype=dt)
+        xd = fe.convert(x, tdt)
+        yd = torch.zeros(n, dtype=torch.float32, device="cuda")
+        for comp in (False, True):
+            if comp:
+                e.compress_cols()
+            ms = _event_ms(lambda: e.run(0, 128, xd, yd, timed=False), reps)
+            err = float(np.linalg.norm(yd.double().cpu().numpy() - y_ref) / np.linalg.norm(y_ref))
+            ib = 2 if comp else 4
+            res["paths"][name + ("+cols16" if comp else "")] = {
+                "ms": round(ms, 4), "gnnz_s": round(nnz / ms / 1e6, 1), "speedup": round((nnz / ms) / base, 3),
+                "gbs": round(((vb + ib) * nnz + (vb + 4 + 4) * n) / ms / 1e6, 1), "rel_err": err}
+        engines[name] = e
+    # CG: b = A x*, x* uniform(-1, 1)
+    xs = fe.uniform_vec(2, 1, n)
+    b = torch.zeros(n, dtype=torch.float64, device="cuda")
+    e64.run(0, 128, xs, b, order=1, timed=False)
+    torch.cuda.synchronize()
+    xc = torch.zeros_like(b)
+    cg = wk.wpk.cg(e64, b, xc, tol=1e-10, max_iter=20000, check_every=16)
+    xi = torch.zeros_like(b)
+    ir = wk.wpk.ir_cg(e64, engines["f32"], b, xi, tol=1e-10, inner_tol=1e-5, max_inner=20000, check_every=16)
+    xb = torch.zeros_like(b)
+    irb = wk.wpk.ir_cg(e64, engines["bf16"], b, xb, tol=1e-10, inner_tol=1e-2, max_inner=20000, check_every=16)
+    res["cg"] = {"fp64_cg": cg, "ir_cg_f32_inner": ir, "ir_cg_bf16_inner": irb,
+                 "ir_f32_speedup": round(cg["seconds"] / ir["seconds"], 3),
+                 "ir_bf16_speedup": round(cg["seconds"] / irb["seconds"], 3)}
+    return res
+
+
+def suite_adjoint(reps):
+    """hex 64^3 (3 dof, seed 4), fp32: forward SpMV vs forward + adjoint
+    (dx = A^T dy and dvals) through the autograd binding's kernels."""
+    import torch
+
+    from warpkernel_gb300 import fe
+    from warpkernel_gb300.autograd import WPKMatrix
+    rp, cols, vals = fe.fe_matrix(3, 64, 64, 64, 3, 1, 4)
+    n, nnz = rp.numel() - 1, cols.numel()
+    x = fe.uniform_vec(4, 0, n).float()
+    dy = fe.uniform_vec(4, 2, n).float()
+    out = {"workload": "hex64_3dof fp32 seed 4", "nrows": n, "nnz": nnz}
+    for order in ("slots", "csr"):
+        v = vals.float()
+        m0 = WPKMatrix(rp, cols, v, kind=2, threshold=81)
+        mat = m0 if order == "csr" else WPKMatrix(rp, cols, m0.to_slots(v), kind=2, threshold=81,
+                                                  value_order="slots")
+        y = torch.zeros(n, dtype=torch.float32, device="cuda")
+
+        def fwd():
+            mat.eng.run(0, 128, x, y, timed=False)
+
+        def adj():
+            mat.adjoint(x, dy)
+
+        tf = _event_ms(fwd, reps)
+        ta = _event_ms(adj, reps)
+        tb = _event_ms(lambda: (fwd(), adj()), reps)
+        out[order] = {"fwd_ms": round(tf, 4), "adj_ms": round(ta, 4), "fwd_plus_adj_ms": round(tb, 4),
+                      "ratio": round(tb / tf, 3), "fused_symmetric_path": mat.symmetric}
+    return out
+
+
+def suite_batched():
+    """512 FE patches (2-D Q1 / 3-D hex, 1k-200k rows, 1 or 3 dof, 1-16 RHS,
+    fp32, seed 3) in one persistent CUDA-graph launch; autotuned threshold
+    and RHS tile (tuned on the first 128 matrices)."""
+    import torch
+
+    from warpkernel_gb300 import batched
+    specs = batched.fe_matrix_set(512, seed=3)
+    tune = batched.autotune(specs, sample=128, reps=3)
+    b = batched.Batch.from_fe(specs, "f32", tune["threshold_frac"], tune["rhs_tile"])
+    X, Y = batched.make_vectors(specs)
+    b.set_vectors(X, Y)
+    b.capture()
+    secs = sorted(b.run() for _ in range(10))
+    med = secs[len(secs) // 2]
+    B = batched.algorithmic_bytes(specs)
+    nnz_rhs = sum(s["nnz"] * s["nrhs"] for s in specs)
+    del b, X, Y
+    torch.cuda.empty_cache()
+    return {"matrices": len(specs), "rows": sum(s["nrows"] for s in specs), "nnz": sum(s["nnz"] for s in specs),
+            "nnz_rhs": nnz_rhs, "ms": round(med * 1e3, 4), "gnnz_rhs_s": round(nnz_rhs / med / 1e9, 2),
+            "gbs": round(B / med / 1e9, 1), "threshold_frac": tune["threshold_frac"], "rhs_tile": tune["rhs_tile"],
+            "launch": "one persistent kernel, CUDA graph replay"}
+
+
+def run_suites(args):
+    import torch
+    out = {}
+    for name, fn in (("mixed_precision_and_cg", lambda: suite_mixed_and_cg(50)),
+                     ("adjoint", lambda: suite_adjoint(50)), ("batched", suite_batched)):
+        t0 = time.time()
+        try:
+            out[name] = fn()
+        except Exception as e:  # a failing suite must not hide the headline
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+        out[name]["wall_s"] = round(time.time() - t0, 2)
+        torch.cuda.empty_cache()
+    return out
 
 
 def run_reference(args):
@@ -311,6 +459,8 @@ def main():
     ap.add_argument("--mesh", type=int, default=128, help="hex elements per axis (128 = the headline)")
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-suites", action="store_true",
+                    help="skip the mixed-precision / CG / adjoint / batched measurements")
     args = ap.parse_args()
     if args.impl == "reference":
         out, rank = run_reference(args)

@@ -301,6 +301,31 @@ wk_status wk_adjoint_transposed_layout(const wk_adjoint *a, wk_layout **tl);
 
 wk_status wk_adjoint_destroy(wk_adjoint *a);
 
+/* ---- batched multi-RHS (no reference counterpart) ------------------------ */
+
+typedef struct wk_batch wk_batch;
+
+/* Many engines (all WK_F32 or all WK_F64; they must outlive the batch), each
+ * with nrhs[m] right-hand sides, computed by one persistent launch: work
+ * items (matrix, `chunk` layout warps) ordered by cost are taken from a
+ * global queue by the warps of one wave of blocks.  Each loaded value and
+ * column is reused for `rhs_tile` right-hand sides (1, 2, 4, 8 or 16).
+ * Results equal each engine's own run (same per-row order), whichever warp
+ * computes them. */
+wk_status wk_batch_create(wk_engine *const *engines, const uint32_t *nrhs, int count, int rhs_tile, int chunk,
+                          wk_batch **out);
+/* X[m]: device, ncols_m x nrhs_m, row-major; Y[m]: device, nrows_m x nrhs_m
+ * (rows without entries are not written). */
+wk_status wk_batch_set_vectors(wk_batch *b, const void *const *X, void *const *Y);
+wk_status wk_batch_set_tile(wk_batch *b, int rhs_tile);
+/* Captures the launch (queue reset + persistent kernel) into a CUDA graph
+ * that wk_batch_run then replays. */
+wk_status wk_batch_capture(wk_batch *b);
+/* One launch; seconds (optional) = device time, synchronous. */
+wk_status wk_batch_run(wk_batch *b, void *stream, float *seconds);
+wk_status wk_batch_info(const wk_batch *b, uint32_t *nitems, uint32_t *grid, int *rhs_tile);
+wk_status wk_batch_destroy(wk_batch *b);
+
 /* ---- verification ------------------------------------------------------- */
 
 /* engine::verify(orig, comp) -- warpkernel.hpp:932-943 (host arrays of nrows

@@ -76,6 +76,13 @@ SIGNATURES = {
     "wk_adjoint_info": (C.c_int, [vp, _ip, C.POINTER(LayoutInfo)]),
     "wk_adjoint_transposed_layout": (C.c_int, [vp, _pvp]),
     "wk_adjoint_destroy": (C.c_int, [vp]),
+    "wk_batch_create": (C.c_int, [vp, _u32p, C.c_int, C.c_int, C.c_int, _pvp]),
+    "wk_batch_set_vectors": (C.c_int, [vp, vp, vp]),
+    "wk_batch_set_tile": (C.c_int, [vp, C.c_int]),
+    "wk_batch_capture": (C.c_int, [vp]),
+    "wk_batch_run": (C.c_int, [vp, vp, _fp]),
+    "wk_batch_info": (C.c_int, [vp, _u32p, _u32p, _ip]),
+    "wk_batch_destroy": (C.c_int, [vp]),
     "wk_verify": (C.c_int, [vp, vp, vp, _ip, _i64p]),
     "wk_verify_x": (C.c_int, [vp, vp, vp, C.c_int, _ip, _i64p]),
     "wk_fe_size": (C.c_int, [C.c_int] * 5 + [_i64p, _i64p]),

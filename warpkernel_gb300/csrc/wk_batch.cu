@@ -1,0 +1,356 @@
+// wk_batch.cu -- many WPK matrices, each with several right-hand sides, in
+// one persistent launch.
+//
+// Work is split into items (matrix, range of layout warps) ordered by cost,
+// largest first; every warp of a persistent grid (one wave of blocks) takes
+// the next item from a global counter.  Which warp computes an item does not
+// change its arithmetic, so results are deterministic.  For each stored slot
+// the value and column are loaded once and reused for an RHS tile of TR
+// right-hand sides: X is row-major (ncols x k), so the TR values of column c
+// are contiguous and are gathered with vector loads.  The counter reset and
+// the kernel are captured once in a CUDA graph and replayed.
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "wk_internal.cuh"
+
+namespace wk {
+namespace {
+
+constexpr int WS = 32;
+constexpr int BATCH_BLOCK = 256;
+
+template <typename T>
+struct BatchMat {
+  const int4 *desc;
+  const T *vals;
+  const int32_t *cols;
+  const int32_t *row_map;
+  const T *X;
+  T *Y;
+  uint32_t nzr, W, k, ld;  // ld = row stride of X and Y (= k)
+};
+
+template <typename T, int TR>
+__device__ __forceinline__ void gather_tile(const T *__restrict__ xr, int jn, bool vec4, T (&g)[TR]) {
+  if constexpr (TR >= 4 && sizeof(T) == 4) {
+    if (vec4) {
+#pragma unroll
+      for (int j = 0; j < TR; j += 4) {
+        if (j < jn) {
+          const float4 f = __ldg(reinterpret_cast<const float4 *>(xr + j));
+          g[j] = f.x; g[j + 1] = f.y; g[j + 2] = f.z; g[j + 3] = f.w;
+        } else {
+          g[j] = g[j + 1] = g[j + 2] = g[j + 3] = T(0);
+        }
+      }
+      return;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < TR; j++) g[j] = j < jn ? __ldg(xr + j) : T(0);
+}
+
+template <typename T, int TR>
+__global__ void __launch_bounds__(BATCH_BLOCK) k_batch(const BatchMat<T> *__restrict__ mats,
+                                                        const int4 *__restrict__ items, uint32_t nitems,
+                                                        unsigned *__restrict__ counter) {
+  const uint32_t lane = threadIdx.x & 31;
+  for (;;) {
+    unsigned it = 0;
+    if (lane == 0) it = atomicAdd(counter, 1u);
+    it = __shfl_sync(0xffffffffu, it, 0);
+    if (it >= nitems) break;
+    const int4 item = items[it];
+    const BatchMat<T> M = mats[item.x];
+    const uint32_t k = M.k, ld = M.ld;
+    const bool vec4 = (ld & 3u) == 0 && ((reinterpret_cast<uintptr_t>(M.X) & 15u) == 0);
+    for (uint32_t w = (uint32_t)item.y; w < (uint32_t)item.z; w++) {
+      const int4 d = M.desc[w];
+      const uint32_t T_ = (uint32_t)d.z, A = (uint32_t)d.y;
+      const uint32_t p = (uint32_t)d.w + lane / T_;
+      const bool valid = p < M.nzr;
+      const size_t o = (size_t)(uint32_t)d.x + lane;
+      for (uint32_t j0 = 0; j0 < k; j0 += TR) {
+        const int jn = (int)min((uint32_t)TR, k - j0);
+        T acc[TR];
+#pragma unroll
+        for (int j = 0; j < TR; j++) acc[j] = T(0);
+        size_t slot = o;
+#pragma unroll 2
+        for (uint32_t i = 0; i < A; i++, slot += WS) {
+          const T v = __ldcs(M.vals + slot);
+          const int c = __ldcs(M.cols + slot);
+          T g[TR];
+          gather_tile<T, TR>(M.X + (size_t)c * ld + j0, jn, vec4, g);
+#pragma unroll
+          for (int j = 0; j < TR; j++) acc[j] = fma(v, g[j], acc[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < TR; j++)
+          for (uint32_t s = 1; s < T_; s <<= 1) acc[j] += __shfl_down_sync(0xffffffffu, acc[j], s);
+        if (valid && (lane & (T_ - 1)) == 0) {
+          T *yr = M.Y + (size_t)M.row_map[p] * ld + j0;
+#pragma unroll
+          for (int j = 0; j < TR; j++)
+            if (j < jn) yr[j] = acc[j];
+        }
+      }
+    }
+  }
+}
+
+}  // namespace
+}  // namespace wk
+
+struct wk_batch {
+  int dtype = WK_F32;
+  int rhs_tile = 8;
+  int chunk = 16;
+  std::vector<wk_engine *> engines;
+  std::vector<uint32_t> nrhs;
+  std::vector<uint32_t> nrows, ncols;
+  wk::DevBuf mats, items, counter;
+  uint32_t nitems = 0;
+  unsigned grid = 0;
+  bool vectors_set = false;
+  cudaGraphExec_t graph = nullptr;
+  cudaStream_t graph_stream = nullptr;
+  ~wk_batch() {
+    if (graph) cudaGraphExecDestroy(graph);
+  }
+};
+
+namespace wk {
+namespace {
+
+template <typename T>
+wk_status launch_batch_t(wk_batch *b, cudaStream_t st) {
+  const BatchMat<T> *mats = b->mats.as<BatchMat<T>>();
+  const int4 *items = b->items.as<int4>();
+  unsigned *ctr = b->counter.as<unsigned>();
+  switch (b->rhs_tile) {
+    case 1: k_batch<T, 1><<<b->grid, BATCH_BLOCK, 0, st>>>(mats, items, b->nitems, ctr); break;
+    case 2: k_batch<T, 2><<<b->grid, BATCH_BLOCK, 0, st>>>(mats, items, b->nitems, ctr); break;
+    case 4: k_batch<T, 4><<<b->grid, BATCH_BLOCK, 0, st>>>(mats, items, b->nitems, ctr); break;
+    case 8: k_batch<T, 8><<<b->grid, BATCH_BLOCK, 0, st>>>(mats, items, b->nitems, ctr); break;
+    case 16: k_batch<T, 16><<<b->grid, BATCH_BLOCK, 0, st>>>(mats, items, b->nitems, ctr); break;
+    default: return set_error(WK_ERR_INVALID, "rhs tile %d not in {1,2,4,8,16}", b->rhs_tile);
+  }
+  WK_CHECK_LAUNCH();
+  return WK_OK;
+}
+
+wk_status launch_batch(wk_batch *b, cudaStream_t st) {
+  WK_CUDA(cudaMemsetAsync(b->counter.p, 0, sizeof(unsigned), st));
+  return b->dtype == WK_F64 ? launch_batch_t<double>(b, st) : launch_batch_t<float>(b, st);
+}
+
+template <typename T>
+int occupancy_blocks(int tile) {
+  int nb = 0;
+  switch (tile) {
+    case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<T, 1>, BATCH_BLOCK, 0); break;
+    case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<T, 2>, BATCH_BLOCK, 0); break;
+    case 4: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<T, 4>, BATCH_BLOCK, 0); break;
+    case 8: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<T, 8>, BATCH_BLOCK, 0); break;
+    default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<T, 16>, BATCH_BLOCK, 0); break;
+  }
+  return nb > 0 ? nb : 1;
+}
+
+// Items: (matrix, [w0, w1)) chunks of `chunk` layout warps, largest cost first
+// (cost = stored slots of the chunk x right-hand sides).
+wk_status build_items(wk_batch *b) {
+  struct It {
+    int m, w0, w1;
+    double cost;
+  };
+  std::vector<It> v;
+  for (size_t m = 0; m < b->engines.size(); m++) {
+    const wk_layout *l = b->engines[m]->layout;
+    const uint32_t W = l->info.nwarps;
+    if (!W) continue;
+    std::vector<int4> desc(W);
+    WK_CUDA(cudaMemcpy(desc.data(), l->d.warp_desc, (size_t)W * sizeof(int4), cudaMemcpyDeviceToHost));
+    for (uint32_t w0 = 0; w0 < W; w0 += (uint32_t)b->chunk) {
+      const uint32_t w1 = std::min(W, w0 + (uint32_t)b->chunk);
+      double slots = 0;
+      for (uint32_t w = w0; w < w1; w++) slots += (double)desc[w].y;
+      v.push_back({(int)m, (int)w0, (int)w1, slots * (double)b->nrhs[m]});
+    }
+  }
+  std::stable_sort(v.begin(), v.end(), [](const It &a, const It &c) { return a.cost > c.cost; });
+  std::vector<int4> h(v.size());
+  for (size_t i = 0; i < v.size(); i++) h[i] = make_int4(v[i].m, v[i].w0, v[i].w1, 0);
+  WK_TRY(b->items.alloc(h.size() * sizeof(int4)));
+  if (!h.empty()) WK_CUDA(cudaMemcpy(b->items.p, h.data(), h.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  b->nitems = (uint32_t)h.size();
+  return WK_OK;
+}
+
+int sm_count() {
+  int dev = 0, n = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  return n > 0 ? n : 1;
+}
+
+wk_status set_grid(wk_batch *b) {
+  const int nb = b->dtype == WK_F64 ? occupancy_blocks<double>(b->rhs_tile) : occupancy_blocks<float>(b->rhs_tile);
+  b->grid = (unsigned)(sm_count() * nb);  // one persistent wave
+  return WK_OK;
+}
+
+void drop_graph(wk_batch *b) {
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
+}
+
+}  // namespace
+}  // namespace wk
+
+using namespace wk;
+
+extern "C" wk_status wk_batch_create(wk_engine *const *engines, const uint32_t *nrhs, int count, int rhs_tile,
+                                     int chunk, wk_batch **out) {
+  if (!out) return set_error(WK_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  if (!engines || !nrhs || count <= 0) return set_error(WK_ERR_INVALID, "empty batch");
+  wk_batch *b = new (std::nothrow) wk_batch();
+  if (!b) return set_error(WK_ERR_ALLOC, "host allocation failed");
+  b->dtype = engines[0]->dtype;
+  b->rhs_tile = rhs_tile > 0 ? rhs_tile : 8;
+  b->chunk = chunk > 0 ? chunk : 16;
+  for (int m = 0; m < count; m++) {
+    wk_engine *e = engines[m];
+    if (!e || e->dtype != b->dtype || (b->dtype != WK_F32 && b->dtype != WK_F64)) {
+      delete b;
+      return set_error(WK_ERR_INVALID, "engine %d: all engines must be WK_F32 or all WK_F64", m);
+    }
+    if (nrhs[m] == 0) {
+      delete b;
+      return set_error(WK_ERR_INVALID, "matrix %d has no right-hand side", m);
+    }
+    b->engines.push_back(e);
+    b->nrhs.push_back(nrhs[m]);
+    b->nrows.push_back(e->layout->info.nrows);
+    b->ncols.push_back(e->ncols);
+  }
+  wk_status s = build_items(b);
+  if (s == WK_OK) s = b->counter.alloc(16);
+  if (s == WK_OK) s = b->mats.alloc((size_t)count * std::max(sizeof(BatchMat<float>), sizeof(BatchMat<double>)));
+  if (s == WK_OK) s = set_grid(b);
+  if (s != WK_OK) {
+    delete b;
+    return s;
+  }
+  *out = b;
+  return WK_OK;
+}
+
+// X[m]: device, ncols_m x nrhs_m row-major; Y[m]: device, nrows_m x nrhs_m.
+extern "C" wk_status wk_batch_set_vectors(wk_batch *b, const void *const *X, void *const *Y) {
+  if (!b || !X || !Y) return set_error(WK_ERR_INVALID, "NULL argument");
+  const size_t n = b->engines.size();
+  if (b->dtype == WK_F64) {
+    std::vector<BatchMat<double>> h(n);
+    for (size_t m = 0; m < n; m++) {
+      const wk_engine *e = b->engines[m];
+      h[m] = {e->layout->d.warp_desc, e->vals.as<double>(), e->cols.as<int32_t>(), e->layout->d.row_map,
+              (const double *)X[m], (double *)Y[m], e->layout->info.nznrows, e->layout->info.nwarps, b->nrhs[m],
+              b->nrhs[m]};
+    }
+    WK_CUDA(cudaMemcpy(b->mats.p, h.data(), n * sizeof(h[0]), cudaMemcpyHostToDevice));
+  } else {
+    std::vector<BatchMat<float>> h(n);
+    for (size_t m = 0; m < n; m++) {
+      const wk_engine *e = b->engines[m];
+      h[m] = {e->layout->d.warp_desc, e->vals.as<float>(), e->cols.as<int32_t>(), e->layout->d.row_map,
+              (const float *)X[m], (float *)Y[m], e->layout->info.nznrows, e->layout->info.nwarps, b->nrhs[m],
+              b->nrhs[m]};
+    }
+    WK_CUDA(cudaMemcpy(b->mats.p, h.data(), n * sizeof(h[0]), cudaMemcpyHostToDevice));
+  }
+  b->vectors_set = true;
+  return WK_OK;
+}
+
+extern "C" wk_status wk_batch_set_tile(wk_batch *b, int rhs_tile) {
+  if (!b) return set_error(WK_ERR_INVALID, "batch is NULL");
+  if (rhs_tile != 1 && rhs_tile != 2 && rhs_tile != 4 && rhs_tile != 8 && rhs_tile != 16)
+    return set_error(WK_ERR_INVALID, "rhs tile %d not in {1,2,4,8,16}", rhs_tile);
+  b->rhs_tile = rhs_tile;
+  drop_graph(b);
+  return set_grid(b);
+}
+
+// One persistent launch (replays the captured graph when there is one).
+// seconds (optional): device time of the launch, synchronous.
+extern "C" wk_status wk_batch_run(wk_batch *b, void *stream, float *seconds) {
+  if (!b) return set_error(WK_ERR_INVALID, "batch is NULL");
+  if (!b->vectors_set) return set_error(WK_ERR_STATE, "wk_batch_set_vectors has not been called");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  if (seconds) {
+    WK_CUDA(cudaEventCreate(&t0));
+    WK_CUDA(cudaEventCreate(&t1));
+    WK_CUDA(cudaEventRecord(t0, st));
+  }
+  wk_status s = WK_OK;
+  if (b->graph) {
+    cudaError_t e = cudaGraphLaunch(b->graph, st);
+    if (e != cudaSuccess) s = set_error(WK_ERR_CUDA, "graph launch: %s", cudaGetErrorString(e));
+  } else {
+    s = launch_batch(b, st);
+  }
+  if (seconds) {
+    cudaEventRecord(t1, st);
+    cudaError_t e = cudaEventSynchronize(t1);
+    float ms = 0.f;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, t0, t1);
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    if (s == WK_OK && e != cudaSuccess) s = set_error(WK_ERR_CUDA, "batch run: %s", cudaGetErrorString(e));
+    *seconds = ms * 1e-3f;
+  }
+  return s;
+}
+
+// Captures the counter reset and the persistent kernel into a CUDA graph
+// that wk_batch_run replays (vectors and tile are baked in: call again after
+// changing them).
+extern "C" wk_status wk_batch_capture(wk_batch *b) {
+  if (!b) return set_error(WK_ERR_INVALID, "batch is NULL");
+  if (!b->vectors_set) return set_error(WK_ERR_STATE, "wk_batch_set_vectors has not been called");
+  drop_graph(b);
+  cudaStream_t cap;
+  WK_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+  cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+  wk_status s = e == cudaSuccess ? launch_batch(b, cap) : set_error(WK_ERR_CUDA, "capture: %s", cudaGetErrorString(e));
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(cap, &g);
+  if (s == WK_OK && e != cudaSuccess) s = set_error(WK_ERR_CUDA, "capture: %s", cudaGetErrorString(e));
+  if (s == WK_OK) {
+    e = cudaGraphInstantiate(&b->graph, g, 0);
+    if (e != cudaSuccess) s = set_error(WK_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+  }
+  if (g) cudaGraphDestroy(g);
+  cudaStreamDestroy(cap);
+  return s;
+}
+
+extern "C" wk_status wk_batch_info(const wk_batch *b, uint32_t *nitems, uint32_t *grid, int *rhs_tile) {
+  if (!b) return set_error(WK_ERR_INVALID, "batch is NULL");
+  if (nitems) *nitems = b->nitems;
+  if (grid) *grid = b->grid;
+  if (rhs_tile) *rhs_tile = b->rhs_tile;
+  return WK_OK;
+}
+
+extern "C" wk_status wk_batch_destroy(wk_batch *b) {
+  delete b;
+  return WK_OK;
+}
