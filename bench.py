@@ -359,15 +359,15 @@ def suite_adjoint(reps):
     return out
 
 
-def suite_batched():
+def suite_batched(count=512, tune=True):
     """512 FE patches (2-D Q1 / 3-D hex, 1k-200k rows, 1 or 3 dof, 1-16 RHS,
     fp32, seed 3) in one persistent CUDA-graph launch; autotuned threshold
     and RHS tile (tuned on the first 128 matrices)."""
     import torch
 
     from warpkernel_gb300 import batched
-    specs = batched.fe_matrix_set(512, seed=3)
-    tune = batched.autotune(specs, sample=128, reps=3)
+    specs = batched.fe_matrix_set(512, seed=3)[:count]
+    tune = batched.autotune(specs, sample=128, reps=3) if tune else {"threshold_frac": 0.5, "rhs_tile": 8}
     b = batched.Batch.from_fe(specs, "f32", tune["threshold_frac"], tune["rhs_tile"])
     X, Y = batched.make_vectors(specs)
     b.set_vectors(X, Y)
@@ -461,7 +461,22 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-suites", action="store_true",
                     help="skip the mixed-precision / CG / adjoint / batched measurements")
+    ap.add_argument("--only", choices=["mixed", "adjoint", "batched"],
+                    help="run one suite alone (profiling cases; --steps = timed repetitions, "
+                         "batched: the first 128 matrices with a fixed threshold / tile)")
     args = ap.parse_args()
+    if args.only:
+        import torch
+        torch.cuda.set_device(0)
+        reps = max(args.steps, 1)
+        if args.only == "mixed":
+            res = suite_mixed_and_cg(reps)
+        elif args.only == "adjoint":
+            res = suite_adjoint(reps)
+        else:
+            res = suite_batched(count=128, tune=False)
+        print(json.dumps({"suite": args.only, **res}), flush=True)
+        return
     if args.impl == "reference":
         out, rank = run_reference(args)
     else:

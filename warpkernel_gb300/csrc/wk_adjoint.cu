@@ -277,8 +277,17 @@ __global__ void __launch_bounds__(ADJ_WARPS * 32) k_adjoint_sym_vec(
 }
 
 // Fused adjoint, slot order: the streaming pattern of the fast SpMV with S
-// slots per lane (S = 4 for fp64, 8 for fp32), 256-bit loads of mirror
-// values and columns, and one 256-bit store of the S gradients per lane.
+// slots per lane (8 for fp32, 4 for fp64: 256-bit loads and stores; measured
+// faster than 4 fp32 slots with 128-bit accesses despite the lower occupancy).
+template <typename T>
+struct AdjSlots {
+  static constexpr int value = core::SlotsPerLane<T>::value;
+};
+#define kAdjS (AdjSlots<T>::value)
+__device__ __forceinline__ void st_words(void *p, const uint32_t (&w)[4]) {
+  asm volatile("st.global.v4.b32 [%0], {%1,%2,%3,%4};" ::"l"(p), "r"(w[0]), "r"(w[1]), "r"(w[2]), "r"(w[3])
+               : "memory");
+}
 __device__ __forceinline__ void st_words(void *p, const uint32_t (&w)[8]) {
   asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "r"(w[0]), "r"(w[1]), "r"(w[2]),
                "r"(w[3]), "r"(w[4]), "r"(w[5]), "r"(w[6]), "r"(w[7])
@@ -296,12 +305,12 @@ __device__ __forceinline__ void put_word(uint32_t *w, int k, double v) {
 template <typename T, typename C>
 __device__ __forceinline__ T adjoint_warp_slots(const int4 d, const C *__restrict__ cp0, int base,
                                                 const T *__restrict__ tv, const typename Pair<T>::type *__restrict__ xdy,
-                                                T *__restrict__ dvals, const T (&dyv)[core::SlotsPerLane<T>::value],
-                                                const int (&elv)[core::SlotsPerLane<T>::value], T dyr, int el,
+                                                T *__restrict__ dvals, const T (&dyv)[kAdjS],
+                                                const int (&elv)[kAdjS], T dyr, int el,
                                                 uint32_t lane, uint64_t pol) {
   using namespace core;
   typedef typename Pair<T>::type P;
-  constexpr int S = SlotsPerLane<T>::value, R = 32 / S;
+  constexpr int S = kAdjS, R = 32 / S;
   const uint32_t A = (uint32_t)d.y;
   const size_t o = (size_t)(uint32_t)d.x;
   T acc[S];
@@ -313,7 +322,7 @@ __device__ __forceinline__ T adjoint_warp_slots(const int4 d, const C *__restric
   T *dp = dvals + o + S * lane;
 #pragma unroll 2
   for (uint32_t u = 0; u < units; u++) {
-    uint32_t wv[S * sizeof(T) / 4], wc[S * sizeof(C) / 4], wd[8];
+    uint32_t wv[S * sizeof(T) / 4], wc[S * sizeof(C) / 4], wd[S * sizeof(T) / 4];
     ld_words(vp, wv, pol);
     ld_words(cp, wc, pol);
     const int step = (int)(u * S + sl);
@@ -357,7 +366,7 @@ __global__ void __launch_bounds__(256) k_adjoint_sym_slots(
     const int32_t *__restrict__ c32, const int4 *__restrict__ cdesc, const T *__restrict__ tv,
     const typename Pair<T>::type *__restrict__ xdy, T *__restrict__ dx, T *__restrict__ dvals) {
   using namespace core;
-  constexpr int S = SlotsPerLane<T>::value, R = 32 / S;
+  constexpr int S = kAdjS, R = 32 / S;
   const uint32_t lane = threadIdx.x & 31;
   const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
   if (w < W) {
