@@ -122,6 +122,13 @@ def max_over_ranks(v, world):
     return float(t.item())
 
 
+def replica_rate(units_per_rank, ms_local, world):
+    """Whole-job rate of `world` independent replicas: all ranks' units over
+    the slowest rank's time (max over ranks)."""
+    ms = max_over_ranks(ms_local, world)
+    return world * units_per_rank / (ms * 1e-3), ms
+
+
 def barrier(world):
     if world > 1:
         import torch.distributed as dist

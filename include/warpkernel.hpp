@@ -128,6 +128,36 @@ class device_array {
   size_t n_ = 0;
 };
 
+/* Host CSR matrix (stands in for cusp::csr_matrix<int, ValueType, host_memory>
+ * with the same member names). */
+template <typename IndexType, typename ValueType>
+struct csr_matrix {
+  uint num_rows = 0, num_cols = 0, num_entries = 0;
+  std::vector<IndexType> row_offsets, column_indices;
+  std::vector<ValueType> values;
+};
+
+/* cusp::io::read_matrix_market_file(A, filename) as the drivers call it
+ * (wpk1.cu:43-48, wpk2.cu:54-57): coordinate real/integer/pattern files,
+ * general / symmetric / skew-symmetric; entries sorted by row, then column. */
+template <typename IndexType, typename ValueType>
+void read_matrix_market_file(csr_matrix<IndexType, ValueType> &A, const char *filename) {
+  static_assert(sizeof(IndexType) == 4, "32-bit indices expected");
+  wk_csr *c = nullptr;
+  check(wk_mm_read(filename, &c));
+  int64_t n = 0, m = 0, z = 0;
+  const int32_t *rp = nullptr, *ci = nullptr;
+  const double *v = nullptr;
+  wk_csr_get(c, &n, &m, &z, &rp, &ci, &v);
+  A.num_rows = (uint)n;
+  A.num_cols = (uint)m;
+  A.num_entries = (uint)z;
+  A.row_offsets.assign(rp, rp + n + 1);
+  A.column_indices.assign(ci, ci + z);
+  A.values.assign(v, v + z);
+  wk_csr_free(c);
+}
+
 /* warpkernel::structure (reference warpkernel.hpp:215-551): WPK1 layout. */
 class structure {
  public:
@@ -175,6 +205,42 @@ class structure {
     check(wk_reorder_columns(h_, reinterpret_cast<const int32_t *>(&colinds[0]), out.data(), nullptr));
     for (size_t i = 0; i < out.size(); i++) colinds[i] = out[i];
   }
+  /* reorder_columns_rowsort (warpkernel.hpp:414-444): renumbered columns
+   * sorted within each CSR row; fills reorder_A_rows with their sources. */
+  template <class Array, class Rows>
+  void reorder_columns_rowsort(Array &colinds, Rows &rows) {
+    (void)rows;  // the layout keeps its own copy of the row offsets
+    std::vector<int32_t> out(nz);
+    reorder_A_rows.resize(nz);
+    check(wk_reorder_columns_rowsort(handle(), reinterpret_cast<const int32_t *>(&colinds[0]), out.data(),
+                                     reorder_A_rows.data(), nullptr));
+    for (size_t i = 0; i < out.size(); i++) colinds[i] = out[i];
+  }
+  /* reorder_values_coalesced_rowsort (warpkernel.hpp:505-515), [CPU] as in
+   * the reference: dvalues[reorder_rows[i]] = values[reorder_A_rows[i]]. */
+  template <class HostArray, typename T>
+  void reorder_values_coalesced_rowsort(HostArray &values, device_array<T> &dvalues) {
+    if (reorder_A_rows.size() != nz) throw error(WK_ERR_STATE, "reorder_columns_rowsort has not been called");
+    std::vector<T> v(allocate_nz, T(0));
+    for (uint i = 0; i < nz; i++) v[reorder_rows[i]] = values[reorder_A_rows[i]];
+    dvalues = v;
+  }
+  /* Layout files (the fields of structure::serialize, warpkernel.hpp:253-269). */
+  void save(const std::string &path) const { check(wk_layout_save(handle(), path.c_str())); }
+  void load(const std::string &path) {
+    wk_layout *l = nullptr;
+    check(wk_layout_load(path.c_str(), nullptr, &l));
+    wk_layout_info i;
+    wk_layout_info_get(l, &i);
+    if (i.kind != kind()) {
+      wk_layout_destroy(l);
+      throw error(WK_ERR_INVALID, path + " holds a layout of the other kind");
+    }
+    release();
+    h_ = l;
+    fetch();
+  }
+
   /* reorder_x (warpkernel.hpp:518-530): device_x[row_map_inv[r]] = x[r]. */
   template <class HostArray, typename T>
   void reorder_x(HostArray &x, device_array<T> &device_x) {
@@ -188,6 +254,7 @@ class structure {
   }
 
  protected:
+  virtual int kind() const { return WK_WPK1; }
   void release() {
     if (h_) wk_layout_destroy(h_);
     h_ = nullptr;
@@ -239,6 +306,7 @@ class structure2 : public structure {
   }
 
  protected:
+  int kind() const override { return WK_WPK2; }
   void fetch() override {
     structure::fetch();
     wk_layout_info i;
@@ -279,6 +347,23 @@ class engine {
     engine *e_;
   };
   colinds_proxy device_colinds{this};
+  /* engine.device_values (warpkernel.hpp:782): readable as a host copy of the
+   * allocate_nz padded values; set_values replaces them. */
+  class values_proxy {
+   public:
+    explicit values_proxy(engine *e) : e_(e) {}
+    std::vector<ValueType> to_host() const {
+      std::vector<ValueType> v(e_->kernel->allocate_nz);
+      check(wk_engine_get_values(e_->handle(), v.data(), v.size()));
+      return v;
+    }
+    operator std::vector<ValueType>() const { return to_host(); }
+
+   private:
+    engine *e_;
+  };
+  values_proxy device_values{this};
+  void set_values(const ValueType *A) { check(wk_engine_set_values(handle(), A, nullptr)); }
 
   explicit engine(structure &k) : kernel(&k) {}
   engine(structure &k, ValueType *A, IndexType *colinds) : kernel(&k) { create(A, colinds); }
@@ -302,6 +387,14 @@ class engine {
   float run_x(int nblocks, int blocksize, ValueType *dx, ValueType *dy) {
     float s = 0.f;
     check(wk_run_x(handle(), nblocks, blocksize, cache ? 1 : 0, order, dx, dy, nullptr, &s));
+    return s;
+  }
+  /* run_assembly<cache>(nblocks, blocksize, dy) (warpkernel.hpp:898-929):
+   * y[row_map[p]] = sum of the stored values of row p. */
+  template <bool cache>
+  float run_assembly(int nblocks, int blocksize, ValueType *dy) {
+    float s = 0.f;
+    check(wk_run_assembly(handle(), nblocks, blocksize, dy, nullptr, &s));
     return s;
   }
 

@@ -77,6 +77,10 @@ typedef struct {
 size_t wk_last_error(char *buf, size_t cap);
 /* Library version string.  No reference counterpart. */
 const char *wk_version(void);
+/* Test hook for the error paths (no reference counterpart): the nth device
+ * allocation the library makes from now on fails with WK_ERR_ALLOC without
+ * calling cudaMalloc; 0 switches it off. */
+void wk_debug_fail_alloc(int nth);
 
 /* ---- scan (layout built on the device) ---------------------------------- */
 
@@ -114,6 +118,17 @@ wk_status wk_reorder_columns_coalesced(const wk_layout *l, const int32_t *cols, 
 /* structure::reorder_columns(colinds) -- warpkernel.hpp:401-412: nz column
  * indices renumbered to sorted order, CSR order kept. */
 wk_status wk_reorder_columns(const wk_layout *l, const int32_t *cols, int32_t *out, void *stream);
+
+/* structure::reorder_columns_rowsort(colinds, rows) -- warpkernel.hpp:414-444
+ * (used by optimize.cu:655, optimize2.cu:749): per CSR row, the renumbered
+ * columns row_map_inv[cols[k]] in ascending order (out_cols, nz entries) and
+ * the CSR position each came from (reorder_A_rows, nz entries), so that
+ * vals[reorder_A_rows[k]] are the matching values.  Square matrices only:
+ * every column must lie in [0, nrows).  Equal columns within a row keep their
+ * CSR order (the reference's std::sort leaves their order unspecified).
+ * Host or device arrays; synchronous. */
+wk_status wk_reorder_columns_rowsort(const wk_layout *l, const int32_t *cols, int32_t *out_cols,
+                                     int32_t *reorder_A_rows, void *stream);
 
 /* structure::reorder_x(x, device_x) -- warpkernel.hpp:518-530:
  * x_out[row_map_inv[r]] = x[r].  dtype WK_F64 / WK_F32 / WK_BF16. */
@@ -193,6 +208,44 @@ wk_status wk_run_x(wk_engine *e, int nblocks, int blocksize, int cache, int orde
  * the fastest copies.  Synchronous. */
 wk_status wk_run_host(wk_engine *e, int mapped, int order, const void *x_host, void *y_host,
                       void *stream);
+
+/* engine::run_assembly<cache>(nblocks, blocksize, dy) -- warpkernel.hpp:898-929
+ * with warpKernel_assembly (warpkernel.hpp:78-100): y[row_map[p]] = the sum of
+ * the stored values of row p (first slot, then += each further slot, in the
+ * reference's order).  WPK2 rows are summed by their threads_per_row lanes
+ * and the same lockstep tree as wk_run (the reference returns -1 for WPK2 and
+ * its WPK1 launch passes five arguments to the six-parameter kernel).  dy:
+ * nrows device values (FP32 for WK_BF16 engines); rows without entries are
+ * not written.  `seconds` as for wk_run. */
+wk_status wk_run_assembly(wk_engine *e, int nblocks, int blocksize, void *dy, void *stream,
+                          float *seconds);
+
+/* ---- files -------------------------------------------------------------- */
+
+/* Saves a layout -- structure::serialize's fields (warpkernel.hpp:253-269:
+ * nrows, nz, allocate_nz, nwarps, ... and the row_map, row_map_inv,
+ * reorder_rows, warp_offsets, max_nz_rows arrays) plus WPK2's
+ * threads_per_row / row_offset_warp and the CSR row offsets -- to a binary
+ * file (little-endian, magic "WPKLAYT1"), so a layout is scanned once and
+ * reloaded.  wk_layout_load rebuilds the layout on the current device from
+ * the file's row offsets and threshold (nmax_per_thread) and accepts the file
+ * only if every array and header field is identical to that scan, so a
+ * corrupt or edited file is refused (WK_ERR_INVALID) before any kernel reads
+ * it. */
+wk_status wk_layout_save(const wk_layout *l, const char *path);
+wk_status wk_layout_load(const char *path, void *stream, wk_layout **out);
+
+/* Matrix Market reader -- the drivers' cusp::io::read_matrix_market_file
+ * (wpk1.cu:43-48, wpk2.cu:54-57): `coordinate` matrices with real, double,
+ * integer or pattern fields (pattern values are 1) and general, symmetric or
+ * skew-symmetric symmetry (the mirror entries are added).  The result is CSR
+ * with columns ascending within each row (duplicates kept, in file order).
+ * wk_csr_get exposes its host arrays until wk_csr_free. */
+typedef struct wk_csr wk_csr;
+wk_status wk_mm_read(const char *path, wk_csr **out);
+wk_status wk_csr_get(const wk_csr *c, int64_t *nrows, int64_t *ncols, int64_t *nnz,
+                     const int32_t **rowptr, const int32_t **cols, const double **vals);
+wk_status wk_csr_free(wk_csr *c);
 
 /* ---- solver building blocks (no reference counterpart) ------------------ */
 

@@ -137,6 +137,38 @@ void ref_run_wpk1(void *hp, const double *pvals, const int *pcols, const double 
   }
 }
 
+/* The reference's structure::reorder_columns_rowsort (warpkernel.hpp:414-444):
+ * out_cols = the reordered colinds, out_src = its reorder_A_rows. */
+void ref_reorder_columns_rowsort(void *hp, const int *cols, const int *rowptr, unsigned nz, unsigned nrows,
+                                 int *out_cols, int *out_src) {
+  handle *h = (handle *)hp;
+  cusp::array1d<int, warpkernel::CPUSpace> c(cols, cols + nz);
+  cusp::array1d<int, warpkernel::CPUSpace> rows(rowptr, rowptr + nrows + 1);
+  h->base()->reorder_columns_rowsort(c, rows);
+  copy_out(c, out_cols);
+  copy_out(h->base()->reorder_A_rows, out_src);
+}
+
+/* warpKernel_assembly (warpkernel.hpp:78-100) for every thread of a WPK1
+ * launch with `wpb` warps per block, with the argument list the kernel
+ * declares (engine::run_assembly, warpkernel.hpp:913-921, passes one fewer
+ * and is not compiled). */
+void ref_assembly_wpk1(void *hp, const double *pvals, double *y, int wpb) {
+  handle *h = (handle *)hp;
+  warpkernel::structure *s = h->base();
+  unsigned nblocks = (s->nwarps + wpb - 1) / wpb;
+  blockDim.x = 32 * wpb;
+  double *A = const_cast<double *>(pvals);
+  for (unsigned b = 0; b < nblocks; b++) {
+    blockIdx.x = b;
+    for (unsigned t = 0; t < blockDim.x; t++) {
+      threadIdx.x = t;
+      warpkernel::warpKernel_assembly<false, double, int>(s->nznrows, A, s->row_map.data(), s->max_nz_rows.data(),
+                                                          s->warp_offsets.data(), y);
+    }
+  }
+}
+
 /* engine::verify / verify_x are members of the engine class, which is not
  * compiled; the oracle restates them (wk_oracle.c). */
 }

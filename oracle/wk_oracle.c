@@ -307,6 +307,73 @@ static void run_any(const wko_layout *l, const double *A, const int32_t *c, cons
   }
 }
 
+/* warpKernel_assembly (warpkernel.hpp:78-100): the lane's slot values
+ * summed in slot order. */
+static double lane_asum(const double *A, int32_t toffset, uint32_t maxrows) {
+  uint32_t maxnz = maxrows * WS + (uint32_t)toffset;
+  double sum = A[toffset];
+  for (toffset += (int32_t)WS; (uint32_t)toffset < maxnz; toffset += (int32_t)WS) sum = sum + A[toffset];
+  return sum;
+}
+
+void wko_assembly_f64(const wko_layout *l, const double *pvals, double *y) {
+  if (l->kind == 1) {
+    for (uint32_t id = 0; id < l->nznrows; id++) {
+      uint32_t w = id / WS, lane = id % WS;
+      y[l->row_map[id]] = lane_asum(pvals, l->warp_offsets[w] + (int32_t)lane, l->max_nz_rows[w]);
+    }
+    return;
+  }
+  for (uint32_t w = 0; w < l->nwarps; w++) {
+    uint32_t T = l->threads_per_row[w], row_start = l->row_offset_warp[w];
+    double s[32];
+    for (uint32_t lane = 0; lane < WS; lane++)
+      s[lane] = row_start + lane / T < l->nznrows
+                    ? lane_asum(pvals, l->warp_offsets[w] + (int32_t)lane, l->max_nz_rows[w])
+                    : 0.0;
+    for (uint32_t lead = 0; lead < WS; lead += T) {
+      uint32_t rowid = row_start + lead / T;
+      if (rowid >= l->nznrows) continue;
+      double t[32];
+      for (uint32_t k = 0; k < T; k++) t[k] = s[lead + k];
+      for (uint32_t i = 1; i < T; i <<= 1)
+        for (uint32_t k = 0; k + i < T; k += 2 * i) t[k] = t[k] + t[k + i];
+      y[l->row_map[rowid]] = t[0];
+    }
+  }
+}
+
+typedef struct {
+  int32_t col, src;
+} rs_pair;
+
+static int rs_cmp(const void *a, const void *b) {
+  const rs_pair *x = (const rs_pair *)a, *y = (const rs_pair *)b;
+  if (x->col != y->col) return x->col < y->col ? -1 : 1;
+  return x->src < y->src ? -1 : (x->src > y->src);
+}
+
+void wko_reorder_columns_rowsort(const wko_layout *l, const int32_t *rowptr, const int32_t *cols,
+                                 int32_t *out_cols, int32_t *out_src) {
+  uint32_t maxlen = 0;
+  for (uint32_t r = 0; r < l->nrows; r++)
+    if ((uint32_t)(rowptr[r + 1] - rowptr[r]) > maxlen) maxlen = (uint32_t)(rowptr[r + 1] - rowptr[r]);
+  rs_pair *t = (rs_pair *)malloc((maxlen ? maxlen : 1) * sizeof(rs_pair));
+  for (uint32_t r = 0; r < l->nrows; r++) {
+    int32_t k0 = rowptr[r], len = rowptr[r + 1] - k0;
+    for (int32_t i = 0; i < len; i++) {
+      t[i].col = l->row_map_inv[cols[k0 + i]];
+      t[i].src = k0 + i;
+    }
+    qsort(t, (size_t)len, sizeof(rs_pair), rs_cmp);
+    for (int32_t i = 0; i < len; i++) {
+      out_cols[k0 + i] = t[i].col;
+      out_src[k0 + i] = t[i].src;
+    }
+  }
+  free(t);
+}
+
 void wko_run_f64(const wko_layout *l, const double *pvals, const int32_t *pcols,
                  const double *x, double *y, int fma_mode) {
   run_any(l, pvals, pcols, x, y, 1, fma_mode);

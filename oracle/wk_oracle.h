@@ -57,6 +57,15 @@ void wko_reorder_columns_coalesced(const wko_layout *l, const int32_t *cols, int
 void wko_reorder_columns(const wko_layout *l, const int32_t *cols, int32_t *out);
 /* reorder_x (warpkernel.hpp:518-530). */
 void wko_reorder_x_f64(const wko_layout *l, const double *x, double *xout);
+/* reorder_columns_rowsort (warpkernel.hpp:414-444): per CSR row the
+ * renumbered columns in ascending order and the CSR position of each
+ * (reorder_A_rows); equal columns keep their CSR order. */
+void wko_reorder_columns_rowsort(const wko_layout *l, const int32_t *rowptr, const int32_t *cols,
+                                 int32_t *out_cols, int32_t *out_src);
+/* warpKernel_assembly (warpkernel.hpp:78-100): y[row_map[id]] = sum of the
+ * row's padded values, first slot then += each further one; WPK2 lanes of a
+ * row are combined by the same lockstep tree as the SpMV. */
+void wko_assembly_f64(const wko_layout *l, const double *pvals, double *y);
 
 /* engine::run / run_x in the documented accumulation order
  * (warpkernel.hpp:53-75, 103-125, 127-168, 170-211).

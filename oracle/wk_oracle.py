@@ -58,6 +58,8 @@ def lib():
         L.wko_reorder_columns_coalesced.argtypes = [lp, _i32p, _i32p]
         L.wko_reorder_columns.argtypes = [lp, _i32p, _i32p]
         L.wko_reorder_x_f64.argtypes = [lp, _f64p, _f64p]
+        L.wko_reorder_columns_rowsort.argtypes = [lp, _i32p, _i32p, _i32p, _i32p]
+        L.wko_assembly_f64.argtypes = [lp, _f64p, _f64p]
         L.wko_run_f64.argtypes = [lp, _f64p, _i32p, _f64p, _f64p, C.c_int]
         L.wko_run_x_f64.argtypes = [lp, _f64p, _i32p, _f64p, _f64p, C.c_int]
         L.wko_run_f64_omp.argtypes = [lp, _f64p, _i32p, _f64p, _f64p, C.c_int]
@@ -190,6 +192,20 @@ class OracleLayout:
         lib().wko_reorder_x_f64(C.byref(self.c), np.ascontiguousarray(x, np.float64), out)
         return out
 
+    def reorder_columns_rowsort(self, rowptr, cols):
+        """warpkernel.hpp:414-444 -> (renumbered row-sorted columns, reorder_A_rows)."""
+        out = np.zeros(self.layout.nz, np.int32)
+        src = np.zeros(self.layout.nz, np.int32)
+        lib().wko_reorder_columns_rowsort(C.byref(self.c), np.ascontiguousarray(rowptr, np.int32),
+                                          np.ascontiguousarray(cols, np.int32), out, src)
+        return out, src
+
+    def assembly(self, pvals, y=None):
+        """warpKernel_assembly (warpkernel.hpp:78-100): row sums of the padded values."""
+        y = np.zeros(self.layout.nrows, np.float64) if y is None else y
+        lib().wko_assembly_f64(C.byref(self.c), np.ascontiguousarray(pvals, np.float64), y)
+        return y
+
     # --- arithmetic ----------------------------------------------------------
     def run(self, pvals, pcols, x, y=None, fma=True):
         y = np.zeros(self.layout.nrows, np.float64) if y is None else y
@@ -293,6 +309,8 @@ class RefLib:
         L.ref_reorder_columns_coalesced.argtypes = [C.c_void_p, _i32p, C.c_uint, _i32p]
         L.ref_reorder_x.argtypes = [C.c_void_p, _f64p, C.c_uint, _f64p]
         L.ref_run_wpk1.argtypes = [C.c_void_p, _f64p, _i32p, _f64p, _f64p, C.c_int, C.c_int]
+        L.ref_reorder_columns_rowsort.argtypes = [C.c_void_p, _i32p, _i32p, C.c_uint, C.c_uint, _i32p, _i32p]
+        L.ref_assembly_wpk1.argtypes = [C.c_void_p, _f64p, _f64p, C.c_int]
         self.L = L
 
     @staticmethod
@@ -347,6 +365,18 @@ class RefStructure:
         self.L.ref_run_wpk1(self.h, np.ascontiguousarray(pvals, np.float64),
                             np.ascontiguousarray(pcols, np.int32),
                             np.ascontiguousarray(x, np.float64), y, int(mapped), int(wpb))
+        return y
+
+    def reorder_columns_rowsort(self, rowptr, cols):
+        out = np.zeros(self.nz, np.int32)
+        src = np.zeros(self.nz, np.int32)
+        self.L.ref_reorder_columns_rowsort(self.h, np.ascontiguousarray(cols, np.int32),
+                                           np.ascontiguousarray(rowptr, np.int32), self.nz, self.nrows, out, src)
+        return out, src
+
+    def assembly_wpk1(self, pvals, wpb=4, y=None):
+        y = np.zeros(self.nrows, np.float64) if y is None else y
+        self.L.ref_assembly_wpk1(self.h, np.ascontiguousarray(pvals, np.float64), y, int(wpb))
         return y
 
     def free(self):

@@ -2,11 +2,14 @@
 // wpk2.cu drivers, compiled against include/warpkernel.hpp (the drop-in
 // surface) and run by tests/test_gpu_cpp_driver.py.
 //
-// Matrix: a finite-element matrix from the library's generator (the reference
-// drivers read a Matrix Market file with CUSP, which is not available).
-// Reference y: a host CSR product (the drivers use CUSP's CSR multiply).
+// Matrix: a Matrix Market file read with warpkernel::read_matrix_market_file
+// (the drivers' cusp::io::read_matrix_market_file), or a finite-element
+// matrix from the library's generator.  Reference y: a host CSR product (the
+// drivers use CUSP's CSR multiply).  After WPK1 and WPK2 it runs the rowsort
+// variant of optimize2.cu:740-796, run_assembly and a layout file round trip.
 //
 //   wpk_driver dim ex ey ez dof [ntests]
+//   wpk_driver --mm file.mtx [ntests]
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -20,11 +23,7 @@
 
 using namespace warpkernel;
 
-struct csr {
-  std::vector<IndexType> row_offsets, column_indices;
-  std::vector<ValueType> values;
-  uint num_rows = 0, num_entries = 0;
-};
+typedef csr_matrix<IndexType, ValueType> csr;
 
 static csr make_matrix(int dim, int ex, int ey, int ez, int dof) {
   int64_t n = 0, z = 0;
@@ -52,13 +51,20 @@ static std::vector<ValueType> csr_multiply(const csr &A, const std::vector<Value
 }
 
 int main(int argc, char **argv) {
-  if (argc < 6) {
-    std::fprintf(stderr, "usage: %s dim ex ey ez dof [ntests]\n", argv[0]);
+  csr A;
+  int ntests = 1;
+  if (argc >= 3 && std::string(argv[1]) == "--mm") {
+    read_matrix_market_file(A, argv[2]);
+    std::printf("Finished Loading %s\n", argv[2]);
+    ntests = argc > 3 ? atoi(argv[3]) : 1;
+  } else if (argc >= 6) {
+    const int dim = atoi(argv[1]), ex = atoi(argv[2]), ey = atoi(argv[3]), ez = atoi(argv[4]), dof = atoi(argv[5]);
+    ntests = argc > 6 ? atoi(argv[6]) : 1;
+    A = make_matrix(dim, ex, ey, ez, dof);
+  } else {
+    std::fprintf(stderr, "usage: %s dim ex ey ez dof [ntests] | --mm file.mtx [ntests]\n", argv[0]);
     return 2;
   }
-  const int dim = atoi(argv[1]), ex = atoi(argv[2]), ey = atoi(argv[3]), ez = atoi(argv[4]), dof = atoi(argv[5]);
-  const int ntests = argc > 6 ? atoi(argv[6]) : 1;
-  csr A = make_matrix(dim, ex, ey, ez, dof);
   uint N = A.num_rows, M = A.num_rows, nz = A.num_entries;
   std::vector<ValueType> x(N);
   srand(1);
@@ -168,6 +174,54 @@ int main(int argc, char **argv) {
         eng.device_colinds = restore_col;
       }
     }
+  }
+  // ---- rowsort variant (optimize2.cu:740-796), run_assembly, layout file ----
+  {
+    structure2 kernel1;
+    kernel1.scan(nz, N, &A.values[0], &A.row_offsets[0], &A.column_indices[0], 4);
+    uint nblocks = (kernel1.nwarps + 3) / 4, blocksize = 4 * WARP_SIZE;
+    std::vector<IndexType> reorder_cols = A.column_indices;
+    kernel1.reorder_columns_rowsort(reorder_cols, A.row_offsets);
+    device_array<ValueType> dreordered_x;
+    kernel1.reorder_x(x, dreordered_x);
+    std::vector<ValueType> A_new_values(nz);
+    for (uint i = 0; i < nz; i++) A_new_values[i] = A.values[kernel1.reorder_A_rows[i]];
+    engine<ValueType, IndexType> eng(kernel1, &A_new_values[0], &reorder_cols[0]);
+    device_array<ValueType> dy(N, 0);
+    eng.run_x<true>(nblocks, blocksize, dreordered_x.data(), dy.data());
+    std::vector<ValueType> ycheck = dy;
+    if (!eng.verify_x(y, ycheck)) {
+      std::printf("WPK2_rex_rowsort failed\n");
+      failures++;
+    }
+    device_array<ValueType> vslots;
+    kernel1.reorder_values_coalesced_rowsort(A.values, vslots);
+    if (vslots.to_host() != eng.device_values.to_host()) {
+      std::printf("reorder_values_coalesced_rowsort differs from the engine's values\n");
+      failures++;
+    }
+    // run_assembly: row sums of the stored values
+    std::vector<ValueType> rowsum(N, 0.0);
+    for (uint r = 0; r < N; r++)
+      for (int k = A.row_offsets[r]; k < A.row_offsets[r + 1]; k++) rowsum[r] += A.values[k];
+    device_array<ValueType> ds(N, 0);
+    eng.run_assembly<true>(nblocks, blocksize, ds.data());
+    std::vector<ValueType> scheck = ds;
+    if (!eng.verify(rowsum, scheck)) {
+      std::printf("run_assembly failed\n");
+      failures++;
+    }
+    // the layout survives a file round trip
+    kernel1.save("wpk_layout.bin");
+    structure2 loaded;
+    loaded.load("wpk_layout.bin");
+    if (loaded.row_map != kernel1.row_map || loaded.reorder_rows != kernel1.reorder_rows ||
+        loaded.warp_offsets != kernel1.warp_offsets || loaded.threads_per_row != kernel1.threads_per_row ||
+        loaded.row_offset_warp != kernel1.row_offset_warp || loaded.allocate_nz != kernel1.allocate_nz) {
+      std::printf("layout file round trip differs\n");
+      failures++;
+    }
+    std::remove("wpk_layout.bin");
   }
   // errors surface as exceptions, not exit(): a malformed CSR
   try {

@@ -1,6 +1,7 @@
 """Regenerates tests/golden/wpk_golden.npz from the reference itself.
 
-The reference's host scan/process/reorder code and its WPK1 kernels
+The reference's host scan/process/reorder code (including
+reorder_columns_rowsort) and its WPK1 SpMV and assembly kernels
 (warpkernel.hpp) are compiled for the CPU by `make -C oracle ref` (needs the
 reference sources) and run here on a fixed set of small matrices.  The
 fixture stores inputs and the reference's outputs, so tests on machines
@@ -97,7 +98,10 @@ def main():
             pcr = s.reorder_columns_coalesced(c)
             xr = s.reorder_x(x)
             data[f"{tag}/pcols_renum"], data[f"{tag}/x_reordered"] = pcr, xr
+            rs_cols, rs_src = s.reorder_columns_rowsort(rp, c)
+            data[f"{tag}/cols_rowsort"], data[f"{tag}/reorder_A_rows"] = rs_cols, rs_src
             if kind == 1 and s.nwarps > 0:
+                data[f"{tag}/y_assembly"] = s.assembly_wpk1(pv)
                 for mode, RL in R.items():
                     s2 = RL.scan(rp, 1, 0)
                     data[f"{tag}/y_run_{mode}"] = s2.run_wpk1(pv, pc, x, mapped=True)

@@ -35,3 +35,20 @@ def test_cpp_driver_wpk1_wpk2(tmp_path):
         r = subprocess.run([exe] + args + ["2"], capture_output=True, text=True, timeout=120)
         assert r.returncode == 0, r.stdout + r.stderr
         assert "driver passed: 0 failure(s)" in r.stdout
+
+
+def test_cpp_driver_matrix_market_rowsort_assembly_layout_file(tmp_path):
+    """The driver reading a Matrix Market file (wpk1.cu:43-48), then the
+    rowsort variant, run_assembly and a layout file round trip."""
+    from oracle import wk_oracle as O
+    from test_formats import _write_mm
+    exe = build_driver(tmp_path)
+    rp, cols, vals = O.fe_matrix(3, 7, 6, 5, 2, value_mode=1, seed=3)
+    n = len(rp) - 1
+    ents = [(r + 1, int(cols[q]) + 1, float(vals[q])) for r in range(n) for q in range(rp[r], rp[r + 1])
+            if cols[q] <= r]
+    p = str(tmp_path / "fe.mtx")
+    _write_mm(p, n, n, ents, sym="symmetric")
+    r = subprocess.run([exe, "--mm", p, "2"], capture_output=True, text=True, timeout=180, cwd=str(tmp_path))
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Finished Loading" in r.stdout and "driver passed: 0 failure(s)" in r.stdout

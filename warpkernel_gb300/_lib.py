@@ -47,6 +47,7 @@ class CGParams(C.Structure):
 SIGNATURES = {
     "wk_last_error": (C.c_size_t, [C.c_char_p, C.c_size_t]),
     "wk_version": (C.c_char_p, []),
+    "wk_debug_fail_alloc": (None, [C.c_int]),
     "wk_scan1": (C.c_int, [vp, u32, u32, vp, _pvp]),
     "wk_scan2": (C.c_int, [vp, u32, u32, i32, vp, _pvp]),
     "wk_layout_info_get": (C.c_int, [vp, C.POINTER(LayoutInfo)]),
@@ -89,6 +90,13 @@ SIGNATURES = {
     "wk_fe_fill": (C.c_int, [C.c_int] * 6 + [u64, vp, vp, vp, vp]),
     "wk_uniform_vec": (C.c_int, [u64, u64, vp, i64, vp]),
     "wk_convert": (C.c_int, [vp, C.c_int, vp, C.c_int, i64, vp]),
+    "wk_reorder_columns_rowsort": (C.c_int, [vp, vp, vp, vp, vp]),
+    "wk_run_assembly": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, _fp]),
+    "wk_layout_save": (C.c_int, [vp, C.c_char_p]),
+    "wk_layout_load": (C.c_int, [C.c_char_p, vp, _pvp]),
+    "wk_mm_read": (C.c_int, [C.c_char_p, _pvp]),
+    "wk_csr_get": (C.c_int, [vp, _i64p, _i64p, _i64p, _pvp, _pvp, _pvp]),
+    "wk_csr_free": (C.c_int, [vp]),
 }
 
 

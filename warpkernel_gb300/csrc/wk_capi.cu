@@ -12,6 +12,8 @@ namespace {
 thread_local std::string g_err;
 }
 
+std::atomic<int> g_alloc_fail_countdown{0};
+
 wk_status set_error(wk_status code, const char *fmt, ...) {
   char buf[1024];
   va_list ap;
@@ -148,6 +150,8 @@ size_t wk_last_error(char *buf, size_t cap) {
 }
 
 const char *wk_version(void) { return "warpkernel_gb300 0.1 (sm_103a)"; }
+
+void wk_debug_fail_alloc(int nth) { g_alloc_fail_countdown.store(nth > 0 ? nth : 0); }
 
 wk_status wk_scan1(const int32_t *rowptr, uint32_t nrows, uint32_t nz, void *stream, wk_layout **out) {
   return scan_common(rowptr, nrows, nz, WK_WPK1, 0, stream, out);

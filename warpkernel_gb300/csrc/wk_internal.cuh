@@ -35,6 +35,11 @@ const std::string &last_error();
 #define WK_CHECK_LAUNCH() WK_CUDA(cudaGetLastError())
 
 // ---- device memory -------------------------------------------------------------
+// Fault injection for the error paths: when positive, the countdown is
+// decremented by every device allocation and the one that brings it to zero
+// fails with WK_ERR_ALLOC instead of calling cudaMalloc (wk_debug_fail_alloc).
+extern std::atomic<int> g_alloc_fail_countdown;
+
 // Owning device buffer (cudaMalloc / cudaFree).
 struct DevBuf {
   void *p = nullptr;
@@ -51,6 +56,8 @@ struct DevBuf {
   wk_status alloc(size_t n) {
     release();
     if (n == 0) n = 16;  // keep a valid pointer for empty arrays
+    if (g_alloc_fail_countdown.load() > 0 && g_alloc_fail_countdown.fetch_sub(1) == 1)
+      return set_error(WK_ERR_ALLOC, "injected allocation failure (%zu bytes)", n);
     cudaError_t e = cudaMalloc(&p, n);
     if (e != cudaSuccess) {
       p = nullptr;

@@ -22,7 +22,7 @@ from ._lib import (WK_BF16, WK_F32, WK_F64, WK_ORDER_EXACT, WK_ORDER_FAST, WK_WP
                    LayoutInfo, check, load)
 
 __all__ = ["structure", "structure2", "engine", "profiler", "stats", "DTYPES",
-           "WK_ORDER_FAST", "WK_ORDER_EXACT"]
+           "WK_ORDER_FAST", "WK_ORDER_EXACT", "csr_matrix", "read_matrix_market_file"]
 
 DTYPES = {"f64": WK_F64, "float64": WK_F64, "f32": WK_F32, "float32": WK_F32,
           "bf16": WK_BF16, "bfloat16": WK_BF16}
@@ -154,6 +154,52 @@ class structure:
         check(load().wk_reorder_columns(self.handle, _ptr(colinds), _ptr(out), _stream_ptr(stream)))
         return out
 
+    def reorder_columns_rowsort(self, colinds, rows=None, out=None, stream=None):
+        """warpkernel.hpp:414-444: nz renumbered columns sorted within each
+        CSR row; sets self.reorder_A_rows to the CSR position each came from
+        (host arrays in, host arrays out; CUDA tensors in, CUDA tensors out).
+        `rows` is accepted for the reference's signature; the layout keeps its
+        own copy of the row offsets."""
+        colinds = _host_or_dev(colinds, np.int32)
+        host = isinstance(colinds, np.ndarray)
+        if out is None:
+            out = np.zeros(self.nz, np.int32) if host else _empty_like_dev(colinds, self.nz)
+        src = np.zeros(self.nz, np.int32) if host else _empty_like_dev(colinds, self.nz)
+        check(load().wk_reorder_columns_rowsort(self.handle, _ptr(colinds), _ptr(out), _ptr(src),
+                                                _stream_ptr(stream)))
+        self.reorder_A_rows = src
+        return out
+
+    def reorder_values_coalesced_rowsort(self, values):
+        """warpkernel.hpp:505-515 ([CPU] in the reference too): the padded
+        slot array new_values[reorder_rows[i]] = values[reorder_A_rows[i]]."""
+        src = getattr(self, "reorder_A_rows", None)
+        if src is None:
+            raise RuntimeError("reorder_columns_rowsort has not been called")
+        src = src if isinstance(src, np.ndarray) else src.cpu().numpy()
+        values = np.asarray(values)
+        out = np.zeros(self.allocate_nz, values.dtype)
+        out[self.reorder_rows] = values[src]
+        return out
+
+    def save(self, path):
+        """Writes the layout (structure::serialize's fields, warpkernel.hpp:253-269)."""
+        check(load().wk_layout_save(self.handle, str(path).encode()))
+
+    def load(self, path, stream=None):
+        """Replaces this structure by a layout written with save(); the file
+        must hold a layout of this class's kind."""
+        h = C.c_void_p()
+        check(load().wk_layout_load(str(path).encode(), _stream_ptr(stream), C.byref(h)))
+        info = LayoutInfo()
+        check(load().wk_layout_info_get(h, C.byref(info)))
+        if info.kind != self.kind:
+            load().wk_layout_destroy(h)
+            raise ValueError(f"{path} holds a WPK{info.kind} layout, not WPK{self.kind}")
+        self._release()
+        self._set(h)
+        return self
+
     def reorder_x(self, x, device_x=None, stream=None):
         """warpkernel.hpp:518-530: device_x[row_map_inv[r]] = x[r].  Returns a
         CUDA tensor unless `device_x` is given."""
@@ -214,6 +260,7 @@ class engine:
         self.kernel = k
         self._h = None
         self.dtype = DTYPES[dtype] if isinstance(dtype, str) else int(dtype)
+        self.ncols = k.nrows if ncols is None else int(ncols)
         if A is None:
             return  # engine(structure&) of the reference: no arrays yet
         A = _host_or_dev(A, {WK_F64: np.float64, WK_F32: np.float32}.get(self.dtype, np.uint16))
@@ -268,7 +315,25 @@ class engine:
     def set_values(self, A, stream=None):
         check(load().wk_engine_set_values(self.handle, _ptr(A), _stream_ptr(stream)))
 
+    _XDT = {WK_F64: "torch.float64", WK_F32: "torch.float32", WK_BF16: "torch.bfloat16"}
+    _YDT = {WK_F64: "torch.float64", WK_F32: "torch.float32", WK_BF16: "torch.float32"}
+
+    def _check_vectors(self, dx, dy, mapped):
+        """Sizes and element types of tensor arguments (raw pointers cannot be
+        checked and are taken as given, as the C ABI does)."""
+        if hasattr(dx, "numel"):
+            if not dx.is_cuda:
+                raise ValueError("dx must be a CUDA tensor (use run_host for host vectors)")
+            if str(dx.dtype) != self._XDT[self.dtype] or dx.numel() < self.ncols:
+                raise ValueError(f"dx must hold >= {self.ncols} values of {self._XDT[self.dtype]}")
+        if hasattr(dy, "numel"):
+            if not dy.is_cuda:
+                raise ValueError("dy must be a CUDA tensor")
+            if str(dy.dtype) != self._YDT[self.dtype] or dy.numel() < self.kernel.nrows:
+                raise ValueError(f"dy must hold >= {self.kernel.nrows} values of {self._YDT[self.dtype]}")
+
     def _run(self, fn, nblocks, blocksize, dx, dy, cache, order, stream, timed):
+        self._check_vectors(dx, dy, True)
         sec = C.c_float(0.0)
         check(fn(self.handle, int(nblocks), int(blocksize), int(cache), int(order), _ptr(dx), _ptr(dy),
                  _stream_ptr(stream), C.byref(sec) if timed else None))
@@ -282,6 +347,15 @@ class engine:
     def run_x(self, nblocks, blocksize, dx, dy, cache=True, order=WK_ORDER_FAST, stream=None, timed=True):
         """engine::run_x<cache>: y'[p] = sorted-row sums (reordered x)."""
         return self._run(load().wk_run_x, nblocks, blocksize, dx, dy, cache, order, stream, timed)
+
+    def run_assembly(self, nblocks, blocksize, dy, cache=True, stream=None, timed=True):
+        """engine::run_assembly<cache>(nblocks, blocksize, dy)
+        (warpkernel.hpp:898-929): y[row_map[p]] = sum of row p's values."""
+        self._check_vectors(None, dy, True)
+        sec = C.c_float(0.0)
+        check(load().wk_run_assembly(self.handle, int(nblocks), int(blocksize), _ptr(dy), _stream_ptr(stream),
+                                     C.byref(sec) if timed else None))
+        return float(sec.value) if timed else None
 
     def run_host(self, x_host, y_host, mapped=True, order=WK_ORDER_FAST, stream=None):
         """H2D of x, run (or run_x with mapped=False), D2H of y in one
@@ -316,6 +390,42 @@ class engine:
         check(load().wk_verify_x(self.kernel.handle, o.ctypes.data, c.ctypes.data, int(strict), C.byref(ok),
                                  C.byref(bad)))
         return bool(ok.value)
+
+
+class csr_matrix:
+    """Host CSR matrix with cusp::csr_matrix's member names."""
+
+    def __init__(self, row_offsets, column_indices, values, num_cols=None):
+        self.row_offsets = np.ascontiguousarray(row_offsets, np.int32)
+        self.column_indices = np.ascontiguousarray(column_indices, np.int32)
+        self.values = np.ascontiguousarray(values)
+        self.num_rows = len(self.row_offsets) - 1
+        self.num_cols = self.num_rows if num_cols is None else int(num_cols)
+        self.num_entries = len(self.column_indices)
+
+
+def read_matrix_market_file(path) -> csr_matrix:
+    """cusp::io::read_matrix_market_file as the drivers call it (wpk1.cu:43-48,
+    wpk2.cu:54-57): coordinate real/integer/pattern, general / symmetric /
+    skew-symmetric, returned as CSR sorted by row, then column.  Runs in the
+    library (no CUDA call)."""
+    L = load()
+    h = C.c_void_p()
+    check(L.wk_mm_read(str(path).encode(), C.byref(h)))
+    try:
+        n, m, z = C.c_int64(), C.c_int64(), C.c_int64()
+        rp, ci, v = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        check(L.wk_csr_get(h, C.byref(n), C.byref(m), C.byref(z), C.byref(rp), C.byref(ci), C.byref(v)))
+
+        def arr(p, cnt, dt):
+            if cnt == 0:
+                return np.zeros(0, dt)
+            return np.ctypeslib.as_array(C.cast(p, C.POINTER(np.ctypeslib.as_ctypes_type(dt))),
+                                         shape=(cnt,)).copy()
+        return csr_matrix(arr(rp, n.value + 1, np.int32), arr(ci, z.value, np.int32),
+                          arr(v, z.value, np.float64), m.value)
+    finally:
+        L.wk_csr_free(h)
 
 
 def _cg_params(tol, max_iter, max_inner, inner_tol, check_every):
