@@ -209,6 +209,15 @@ wk_status wk_run_x(wk_engine *e, int nblocks, int blocksize, int cache, int orde
 wk_status wk_run_host(wk_engine *e, int mapped, int order, const void *x_host, void *y_host,
                       void *stream);
 
+/* `count` SpMVs on host vectors, each as wk_run_host (x_host[i] -> device,
+ * run or run_x, y -> y_host[i]) with the same results, but double-buffered
+ * on two copy streams: the upload of x_host[i+1] and the download of
+ * y_host[i-1] overlap SpMV i, so with pinned buffers the host link is hidden
+ * behind the HBM-bound SpMV.  Synchronous: returns when every y_host[i] is
+ * written; `seconds` (optional) = elapsed time of the whole sequence. */
+wk_status wk_run_host_stream(wk_engine *e, int mapped, int order, int count, const void *const *x_host,
+                             void *const *y_host, void *stream, float *seconds);
+
 /* engine::run_assembly<cache>(nblocks, blocksize, dy) -- warpkernel.hpp:898-929
  * with warpKernel_assembly (warpkernel.hpp:78-100): y[row_map[p]] = the sum of
  * the stored values of row p (first slot, then += each further slot, in the

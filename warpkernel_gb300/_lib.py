@@ -66,6 +66,7 @@ SIGNATURES = {
     "wk_run": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, _fp]),
     "wk_run_x": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, _fp]),
     "wk_run_host": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, vp]),
+    "wk_run_host_stream": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, _pvp, _pvp, vp, _fp]),
     "wk_residual": (C.c_int, [vp, vp, vp, vp, vp, vp]),
     "wk_residual_static": (C.c_int, [vp, vp, vp, vp, vp, vp]),
     "wk_cg": (C.c_int, [vp, vp, vp, C.POINTER(CGParams), vp]),

@@ -359,8 +359,10 @@ __device__ __forceinline__ T adjoint_warp_slots(const int4 d, const C *__restric
   return s0 + tail;
 }
 
+// Four resident blocks per SM (64 registers, a few spilled) measured 4 %
+// faster than the unconstrained 76-register build (hex 64^3, fp32).
 template <typename T, bool COMP>
-__global__ void __launch_bounds__(256) k_adjoint_sym_slots(
+__global__ void __launch_bounds__(256, 4) k_adjoint_sym_slots(
     const int4 *__restrict__ desc, uint32_t W, const int32_t *__restrict__ row_map, const uint32_t *__restrict__ slen,
     uint32_t nzr, uint32_t nrows, const int32_t *__restrict__ pc, const uint16_t *__restrict__ c16,
     const int32_t *__restrict__ c32, const int4 *__restrict__ cdesc, const T *__restrict__ tv,

@@ -416,6 +416,87 @@ wk_status wk_run_host(wk_engine *e, int mapped, int order, const void *x_host, v
   return WK_OK;
 }
 
+namespace {
+// Streams and events of one wk_run_host_stream call, released on every exit.
+struct HostStreamRes {
+  cudaStream_t h2d = nullptr, d2h = nullptr;
+  cudaEvent_t ev[7] = {};  // h2d done [2], SpMV done [2], d2h done [2], start
+  ~HostStreamRes() {
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+    if (h2d) cudaStreamDestroy(h2d);
+    if (d2h) cudaStreamDestroy(d2h);
+  }
+};
+}  // namespace
+
+wk_status wk_run_host_stream(wk_engine *e, int mapped, int order, int count, const void *const *x_host,
+                             void *const *y_host, void *stream, float *seconds) {
+  if (!e || count < 0 || (count && (!x_host || !y_host))) return set_error(WK_ERR_INVALID, "NULL argument");
+  for (int i = 0; i < count; i++)
+    if (!x_host[i] || !y_host[i]) return set_error(WK_ERR_INVALID, "vector %d is NULL", i);
+  cudaStream_t st = S(stream);
+  const size_t xb = (size_t)e->ncols * dtype_size(e->dtype);
+  const size_t yb = (size_t)e->layout->info.nrows * (e->dtype == WK_F64 ? 8 : 4);
+  if (!e->xbuf.p) WK_TRY(e->xbuf.alloc(xb));
+  if (!e->ybuf.p) WK_TRY(e->ybuf.alloc(yb));
+  if (!e->xbuf2.p) WK_TRY(e->xbuf2.alloc(xb));
+  if (!e->ybuf2.p) WK_TRY(e->ybuf2.alloc(yb));
+  wk::DevBuf *xs[2] = {&e->xbuf, &e->xbuf2}, *ys[2] = {&e->ybuf, &e->ybuf2};
+  HostStreamRes r;
+  WK_CUDA(cudaStreamCreateWithFlags(&r.h2d, cudaStreamNonBlocking));
+  WK_CUDA(cudaStreamCreateWithFlags(&r.d2h, cudaStreamNonBlocking));
+  for (int k = 0; k < 6; k++) WK_CUDA(cudaEventCreateWithFlags(&r.ev[k], cudaEventDisableTiming));
+  cudaEvent_t *h2d_done = r.ev, *run_done = r.ev + 2, *d2h_done = r.ev + 4;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  if (seconds) {
+    WK_CUDA(cudaEventCreate(&r.ev[6]));
+    t0 = r.ev[6];
+    WK_CUDA(cudaEventRecord(t0, st));
+  }
+  // empty rows are never written by the SpMV: zero both staging vectors once
+  if (e->layout->info.nznrows < e->layout->info.nrows)
+    for (int b = 0; b < 2; b++) WK_CUDA(cudaMemsetAsync(ys[b]->p, 0, yb, st));
+  WK_CUDA(cudaEventRecord(run_done[0], st));  // uploads start after the memsets
+  WK_CUDA(cudaEventRecord(run_done[1], st));
+  WK_CUDA(cudaStreamWaitEvent(r.h2d, run_done[0], 0));
+  for (int i = 0; i < count; i++) {
+    const int b = i & 1;
+    // x_i into buffer b once SpMV i-2 (its last reader) is done
+    if (i >= 2) WK_CUDA(cudaStreamWaitEvent(r.h2d, run_done[b], 0));
+    if (xb) WK_CUDA(cudaMemcpyAsync(xs[b]->p, x_host[i], xb, cudaMemcpyHostToDevice, r.h2d));
+    WK_CUDA(cudaEventRecord(h2d_done[b], r.h2d));
+    // SpMV i after its upload and after y_{i-2} left buffer b
+    WK_CUDA(cudaStreamWaitEvent(st, h2d_done[b], 0));
+    if (i >= 2) WK_CUDA(cudaStreamWaitEvent(st, d2h_done[b], 0));
+    RunArgs a{e, 0, 0, 1, order, mapped != 0, xs[b]->p, ys[b]->p, st};
+    WK_TRY(launch_spmv(a));
+    WK_CUDA(cudaEventRecord(run_done[b], st));
+    WK_CUDA(cudaStreamWaitEvent(r.d2h, run_done[b], 0));
+    if (yb) WK_CUDA(cudaMemcpyAsync(y_host[i], ys[b]->p, yb, cudaMemcpyDeviceToHost, r.d2h));
+    WK_CUDA(cudaEventRecord(d2h_done[b], r.d2h));
+  }
+  if (count) {
+    WK_CUDA(cudaStreamWaitEvent(st, d2h_done[(count - 1) & 1], 0));
+    if (count > 1) WK_CUDA(cudaStreamWaitEvent(st, d2h_done[count & 1], 0));
+  }
+  if (seconds) {
+    WK_CUDA(cudaEventCreate(&t1));
+    cudaEventRecord(t1, st);
+  }
+  cudaError_t ce = cudaStreamSynchronize(st);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(r.d2h);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(r.h2d);
+  if (ce == cudaSuccess && seconds) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, t0, t1);
+    *seconds = ms * 1e-3f;
+  }
+  if (t1) cudaEventDestroy(t1);
+  if (ce != cudaSuccess) return set_error(WK_ERR_CUDA, "run_host_stream: %s", cudaGetErrorString(ce));
+  return WK_OK;
+}
+
 wk_status wk_verify(const wk_layout *l, const double *orig, const double *comp, int *pass, int64_t *first_bad) {
   if (!l || !orig || !comp || !pass) return set_error(WK_ERR_INVALID, "NULL argument");
   const uint32_t n = l->info.nrows;

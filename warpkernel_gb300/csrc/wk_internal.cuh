@@ -127,6 +127,7 @@ struct wk_engine {
   wk::DevBuf cols;   // allocate_nz int32 column indices (padding 0)
   wk::DevBuf status; // device status word for kernels that can report errors
   wk::DevBuf xbuf, ybuf;  // staging vectors of wk_run_host (allocated on first use)
+  wk::DevBuf xbuf2, ybuf2;  // second staging pair of wk_run_host_stream (double buffering)
   wk::DevBuf scratch;     // per-block partial sums of the solver kernels (grown on demand)
   // compressed columns (wk_engine_compress_cols): 16-bit offsets per slot,
   // compact 32-bit indices of the warps whose span needs them, per-warp descriptor

@@ -365,6 +365,20 @@ class engine:
                                  _stream_ptr(stream)))
         return y_host
 
+    def run_host_stream(self, xs, ys, mapped=True, order=WK_ORDER_FAST, stream=None):
+        """run_host over a sequence of host vectors with the copies of
+        neighbouring steps overlapping each SpMV (double-buffered); returns
+        the elapsed seconds of the whole sequence."""
+        if len(xs) != len(ys):
+            raise ValueError("xs and ys must have the same length")
+        n = len(xs)
+        xp = (C.c_void_p * max(n, 1))(*[_ptr(x) for x in xs])
+        yp = (C.c_void_p * max(n, 1))(*[_ptr(y) for y in ys])
+        sec = C.c_float(0.0)
+        check(load().wk_run_host_stream(self.handle, int(mapped), int(order), n, xp, yp, _stream_ptr(stream),
+                                        C.byref(sec)))
+        return float(sec.value)
+
     def residual(self, x, b, r, norm2=None, stream=None):
         """r = b - A x (fp64 engine, device tensors); norm2: optional 1-element
         float64 CUDA tensor receiving ||r||^2."""
