@@ -408,11 +408,78 @@ def suite_batched(count=512, tune=True):
             "launch": "one persistent kernel, CUDA graph replay"}
 
 
+def powerlaw_csr(n, seed=5, zipf=1.6, maxlen=2000, band=4096):
+    """Seeded skewed matrix: row lengths from a Zipf law (1..maxlen), columns
+    uniform within a band around the diagonal (unsorted, duplicates allowed)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    lens = np.minimum(rng.zipf(zipf, n), maxlen).astype(np.int64)
+    rp = np.zeros(n + 1, np.int64)
+    rp[1:] = np.cumsum(lens)
+    rows = np.repeat(np.arange(n, dtype=np.int64), lens)
+    cols = np.clip(rows + rng.integers(-band, band + 1, int(rp[-1])), 0, n - 1)
+    vals = rng.uniform(-1, 1, int(rp[-1]))
+    return rp.astype(np.int32), cols.astype(np.int32), vals
+
+
+def suite_ablation(reps):
+    """The optimization.cu ablation on GB300: WPK1 (sorted, interleaved) vs
+    scan_nosort, scan_nocoalesced and both, fp64 run, on the hex 64^3 FE matrix
+    (near-uniform rows) and a seeded power-law matrix (skewed rows); WPK2 at
+    the best of a few thresholds beside them.  GB/s counts the matrix's own
+    12 B/nnz + 20 B/row, so padding shows up as lost throughput."""
+    import torch
+
+    import warpkernel_gb300 as wk
+    from warpkernel_gb300 import fe
+    out = {}
+    mats = {"hex64_3dof": None, "powerlaw_1M": None}
+    for name in mats:
+        if name == "hex64_3dof":
+            rp, cols, vals = (t.cpu().numpy() for t in fe.fe_matrix(3, 64, 64, 64, 3, 1, 4))
+        else:
+            rp, cols, vals = powerlaw_csr(1 << 20)
+        n, nnz = len(rp) - 1, len(cols)
+        x = fe.uniform_vec(4, 0, n)
+        y = torch.zeros(n, dtype=torch.float64, device="cuda")
+        B = alg_bytes(n, nnz)
+        rows = {}
+
+        def timed(eng, order):
+            return _event_ms(lambda: eng.run(0, 128, x, y, order=order, timed=False), reps)
+
+        for label, flags in (("wpk1", 0), ("nosort", 1), ("nocoalesced", 2), ("nocoalesced_nosort", 3)):
+            k = wk.structure().scan_ablation(nnz, n, rp, flags) if flags else wk.structure().scan(nnz, n, None, rp)
+            eng = wk.engine(k, vals, cols)
+            r = {"padding": round(k.allocate_nz / nnz, 4)}
+            for oname, order in (("exact", 1), ("fast", 0)):
+                if flags & 2 and order == 0:
+                    continue  # one order only
+                ms = timed(eng, order)
+                r[oname] = {"ms": round(ms, 4), "gbs": round(B / ms / 1e6, 1)}
+            rows[label] = r
+            del eng, k
+        best = None
+        for th in (8, 32, 81, 256):
+            k = wk.structure2().scan(nnz, n, None, rp, None, th)
+            eng = wk.engine(k, vals, cols)
+            ms = timed(eng, 0)
+            if best is None or ms < best["ms"]:
+                best = {"threshold": th, "ms": round(ms, 4), "gbs": round(B / ms / 1e6, 1),
+                        "padding": round(k.allocate_nz / nnz, 4)}
+            del eng, k
+        rows["wpk2_best_fast"] = best
+        out[name] = {"nrows": n, "nnz": nnz, **rows}
+        torch.cuda.empty_cache()
+    return out
+
+
 def run_suites(args):
     import torch
     out = {}
     for name, fn in (("mixed_precision_and_cg", lambda: suite_mixed_and_cg(50)),
-                     ("adjoint", lambda: suite_adjoint(50)), ("batched", suite_batched)):
+                     ("adjoint", lambda: suite_adjoint(50)), ("batched", suite_batched),
+                     ("ablation", lambda: suite_ablation(20))):
         t0 = time.time()
         try:
             out[name] = fn()
@@ -485,7 +552,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-suites", action="store_true",
                     help="skip the mixed-precision / CG / adjoint / batched measurements")
-    ap.add_argument("--only", choices=["mixed", "adjoint", "batched"],
+    ap.add_argument("--only", choices=["mixed", "adjoint", "batched", "ablation"],
                     help="run one suite alone (profiling cases; --steps = timed repetitions, "
                          "batched: the first 128 matrices with a fixed threshold / tile)")
     args = ap.parse_args()
@@ -497,6 +564,8 @@ def main():
             res = suite_mixed_and_cg(reps)
         elif args.only == "adjoint":
             res = suite_adjoint(reps)
+        elif args.only == "ablation":
+            res = suite_ablation(reps)
         else:
             res = suite_batched(count=128, tune=False)
         print(json.dumps({"suite": args.only, **res}), flush=True)

@@ -173,6 +173,7 @@ class structure {
   std::vector<int> warp_offsets;
   std::vector<uint> max_nz_rows;
   uint nrows = 0, nznrows = 0, nz = 0, allocate_nz = 0, nwarps = 0;
+  uint variant = 0;  // WK_ABL_* flags of an ablation layout
 
   /* structure::scan (warpkernel.hpp:309-365): only `rows` is read. */
   template <typename ValueType, typename IndexType>
@@ -182,6 +183,17 @@ class structure {
     (void)colinds;
     release();
     check(wk_scan1(reinterpret_cast<const int32_t *>(rows), nrows_, nz_, nullptr, &h_));
+    fetch();
+  }
+  /* The WPK1 ablation layouts of optimization.cu: flags WK_ABL_NOSORT
+   * (scan_nosort), WK_ABL_NOCOALESCE (scan_nocoalesced) or both
+   * (scan_nocoalesced_nosort). */
+  template <typename IndexType>
+  void scan_ablation(uint &nz_, uint &nrows_, IndexType *rows, int flags) {
+    static_assert(sizeof(IndexType) == 4, "32-bit row offsets expected");
+    if (kind() != WK_WPK1) throw error(WK_ERR_INVALID, "the ablation layouts are WPK1 layouts");
+    release();
+    check(wk_scan1_ablation(reinterpret_cast<const int32_t *>(rows), nrows_, nz_, flags, nullptr, &h_));
     fetch();
   }
   /* scan of a CSR container with row_offsets / column_indices / values. */
@@ -274,6 +286,7 @@ class structure {
     nz = i.nz;
     allocate_nz = i.allocate_nz;
     nwarps = i.nwarps;
+    variant = i.variant;
     get(WK_FIELD_ROW_MAP, row_map);
     get(WK_FIELD_ROW_MAP_INV, row_map_inv);
     get(WK_FIELD_REORDER_ROWS, reorder_rows);

@@ -68,6 +68,7 @@ typedef struct {
   uint32_t nrows, nznrows, nz, allocate_nz, nwarps;
   uint32_t min_nz, max_nz;   /* WPK2: extreme non-empty row lengths */
   uint32_t nmax_per_thread;  /* WPK2: the threshold it was scanned with */
+  uint32_t variant;          /* WK_ABL_* flags of wk_scan1_ablation, else 0 */
 } wk_layout_info;
 
 /* ---- diagnostics ------------------------------------------------------- */
@@ -96,6 +97,26 @@ wk_status wk_scan1(const int32_t *rowptr, uint32_t nrows, uint32_t nz, void *str
  * warpkernel.hpp:579-736.  Same inputs plus the per-thread threshold. */
 wk_status wk_scan2(const int32_t *rowptr, uint32_t nrows, uint32_t nz, int32_t threshold,
                    void *stream, wk_layout **out);
+
+/* The WPK1 ablation layouts of optimization.cu, built on the device:
+ * WK_ABL_NOSORT -- scan_nosort (optimization.cu:372-442): rows keep their CSR
+ *   order (warps of 32 consecutive rows, each padded to its longest row);
+ * WK_ABL_NOCOALESCE -- scan_nocoalesced (233-294): sorted rows, but each
+ *   lane's entries are contiguous (slot o_w + lane * max_nz_rows[w] + i)
+ *   instead of interleaved;
+ * both -- scan_nocoalesced_nosort (298-368).
+ * Rows without entries are moved to the end and get no warp, as in
+ * structure::scan (the optimization.cu scans count warps over all rows, and
+ * their nosort forms read past their row list when a row is empty).  Layouts
+ * with WK_ABL_NOSORT only are ordinary interleaved WPK1 layouts that every
+ * call accepts.  WK_ABL_NOCOALESCE layouts support engine creation and
+ * access, the reorderings, run / run_x (the reference's
+ * warpKernel_nocoalesced, optimization.cu:91-114, in either order argument),
+ * run_host and the files; the solver, adjoint, batched, compressed-column
+ * and assembly calls refuse them with WK_ERR_INVALID. */
+enum { WK_ABL_NOSORT = 1, WK_ABL_NOCOALESCE = 2 };
+wk_status wk_scan1_ablation(const int32_t *rowptr, uint32_t nrows, uint32_t nz, int flags, void *stream,
+                            wk_layout **out);
 
 wk_status wk_layout_info_get(const wk_layout *l, wk_layout_info *info);
 

@@ -105,6 +105,79 @@ int wko_scan1(const int32_t *rowptr, uint32_t nrows, uint32_t nz, wko_layout *l)
   return 0;
 }
 
+/* The row order of optimization.cu's nosort scans (311-318, 385-392): rows
+ * with entries in CSR order, then the empty rows in CSR order. */
+static pair_t *unsorted_rows(const int32_t *rowptr, wko_layout *l) {
+  uint32_t n = l->nrows;
+  pair_t *nnz_r = (pair_t *)malloc((size_t)(n ? n : 1) * sizeof(pair_t));
+  l->row_map = (int32_t *)malloc((size_t)(n ? n : 1) * sizeof(int32_t));
+  l->row_map_inv = (int32_t *)malloc((size_t)(n ? n : 1) * sizeof(int32_t));
+  if (!nnz_r || !l->row_map || !l->row_map_inv) {
+    free(nnz_r);
+    return NULL;
+  }
+  uint32_t p = 0;
+  for (int pass = 0; pass < 2; pass++)
+    for (uint32_t r = 0; r < n; r++) {
+      uint32_t len = (uint32_t)(rowptr[r + 1] - rowptr[r]);
+      if ((len > 0) != (pass == 0)) continue;
+      nnz_r[p].row = r;
+      nnz_r[p].len = len;
+      p++;
+    }
+  l->nznrows = 0;
+  for (uint32_t q = 0; q < n; q++) {
+    if (nnz_r[q].len > 0) l->nznrows++;
+    l->row_map[q] = (int32_t)nnz_r[q].row;
+    l->row_map_inv[nnz_r[q].row] = (int32_t)q;
+  }
+  return nnz_r;
+}
+
+/* optimization.cu scan_nosort / scan_nocoalesced / scan_nocoalesced_nosort:
+ * the warp tables of structure::scan over the chosen row order; entry i of
+ * the row in lane l of warp w goes to o_w + l + 32 i (interleaved) or to
+ * o_w + l * A_w + i (optimization.cu:289-290, 363-364, 437-438). */
+int wko_scan1_ablation(const int32_t *rowptr, uint32_t nrows, uint32_t nz, int flags, wko_layout *l) {
+  memset(l, 0, sizeof(*l));
+  l->kind = 1;
+  l->nrows = nrows;
+  l->nz = nz;
+  l->variant = (uint32_t)flags;
+  if (flags & ~(WKO_ABL_NOSORT | WKO_ABL_NOCOALESCE)) return 1;
+  if (check_csr(rowptr, nrows, nz)) return 1;
+  pair_t *nnz_r = (flags & WKO_ABL_NOSORT) ? unsorted_rows(rowptr, l) : sort_rows(rowptr, l);
+  if (!nnz_r) return 2;
+  uint32_t W = (l->nznrows + WS - 1) / WS;
+  l->nwarps = W;
+  l->max_nz_rows = (uint32_t *)calloc(W ? W : 1, sizeof(uint32_t));
+  l->warp_offsets = (int32_t *)calloc(W + 1, sizeof(int32_t));
+  l->reorder_rows = (uint32_t *)calloc(nz ? nz : 1, sizeof(uint32_t));
+  if (!l->max_nz_rows || !l->warp_offsets || !l->reorder_rows) {
+    free(nnz_r);
+    return 2;
+  }
+  for (uint32_t w = 0; w < W; w++) {
+    uint32_t mx = 0;
+    for (uint32_t r = WS * w; r < l->nznrows && r < WS * (w + 1); r++)
+      if (nnz_r[r].len > mx) mx = nnz_r[r].len;
+    l->max_nz_rows[w] = mx;
+  }
+  for (uint32_t w = 0; w < W; w++)
+    l->warp_offsets[w + 1] = (int32_t)((uint32_t)l->warp_offsets[w] + l->max_nz_rows[w] * WS);
+  l->allocate_nz = (uint32_t)l->warp_offsets[W];
+  for (uint32_t w = 0; w < W; w++)
+    for (uint32_t rs = WS * w; rs < l->nznrows && rs < WS * (w + 1); rs++) {
+      uint32_t r = nnz_r[rs].row, len = nnz_r[rs].len, lane = rs % WS;
+      for (uint32_t i = 0; i < len; i++)
+        l->reorder_rows[rowptr[r] + i] = (flags & WKO_ABL_NOCOALESCE)
+                                             ? (uint32_t)l->warp_offsets[w] + lane * l->max_nz_rows[w] + i
+                                             : (uint32_t)l->warp_offsets[w] + lane + i * WS;
+    }
+  free(nnz_r);
+  return 0;
+}
+
 /* structure2::scan, WPK2 (warpkernel.hpp:579-736).  The reference splits
  * warps by inserting copies in front of the current element of three
  * std::vectors (633-691); the copies are identical, so appending them in
@@ -291,8 +364,35 @@ static void wpk2_warp(const wko_layout *l, uint32_t w, const double *A, const in
   }
 }
 
+/* warpKernel_nocoalesced (optimization.cu:91-114): the lane's entries are
+ * contiguous. */
+static double lane_sum_nc(const double *A, const int32_t *c, const double *x, int32_t toffset,
+                          uint32_t maxrows, int fma_mode) {
+  int32_t end = toffset + (int32_t)maxrows;
+  double sum = A[toffset] * x[c[toffset]];
+  for (toffset++; toffset < end; toffset++) {
+    if (fma_mode)
+      sum = fma(A[toffset], x[c[toffset]], sum);
+    else
+      sum = sum + A[toffset] * x[c[toffset]];
+  }
+  return sum;
+}
+
 static void run_any(const wko_layout *l, const double *A, const int32_t *c, const double *x,
                     double *y, int mapped, int fma_mode) {
+  if (l->kind == 1 && (l->variant & WKO_ABL_NOCOALESCE)) {
+    for (uint32_t id = 0; id < l->nznrows; id++) {
+      uint32_t w = id / WS, lane = id % WS;
+      double sum = lane_sum_nc(A, c, x, l->warp_offsets[w] + (int32_t)(lane * l->max_nz_rows[w]),
+                               l->max_nz_rows[w], fma_mode);
+      if (mapped)
+        y[l->row_map[id]] = sum;
+      else
+        y[id] = sum;
+    }
+    return;
+  }
   if (l->kind == 1) {
     for (uint32_t id = 0; id < l->nznrows; id++) {
       uint32_t w = id / WS, lane = id % WS;

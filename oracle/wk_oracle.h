@@ -30,6 +30,7 @@ typedef struct {
   int kind;                   /* 1 = WPK1, 2 = WPK2 */
   uint32_t nrows, nznrows, nz, allocate_nz, nwarps;
   uint32_t min_nz, max_nz, nmax_per_thread; /* WPK2 only */
+  uint32_t variant;           /* WKO_ABL_* flags of wko_scan1_ablation, else 0 */
   int32_t *row_map;           /* [nrows]   sorted position -> original row */
   int32_t *row_map_inv;       /* [nrows]   original row -> sorted position */
   uint32_t *reorder_rows;     /* [nz]      CSR position -> padded slot      */
@@ -45,6 +46,14 @@ int wko_scan1(const int32_t *rowptr, uint32_t nrows, uint32_t nz, wko_layout *ou
 int wko_scan2(const int32_t *rowptr, uint32_t nrows, uint32_t nz, int32_t threshold,
               wko_layout *out);
 void wko_free(wko_layout *l);
+
+/* The WPK1 ablation layouts of optimization.cu: WKO_ABL_NOSORT = scan_nosort
+ * (372-442), WKO_ABL_NOCOALESCE = scan_nocoalesced (233-294), both =
+ * scan_nocoalesced_nosort (298-368).  Rows without entries go last and get
+ * no warp (as structure::scan), where the optimization.cu scans count warps
+ * over all rows; on matrices without empty rows the arrays are the same. */
+enum { WKO_ABL_NOSORT = 1, WKO_ABL_NOCOALESCE = 2 };
+int wko_scan1_ablation(const int32_t *rowptr, uint32_t nrows, uint32_t nz, int flags, wko_layout *out);
 
 /* structure::reorder (warpkernel.hpp:380-398): padded values/colinds. */
 void wko_process_f64(const wko_layout *l, const double *vals, const int32_t *cols,

@@ -31,6 +31,7 @@ class _Layout(C.Structure):
         ("nrows", C.c_uint32), ("nznrows", C.c_uint32), ("nz", C.c_uint32),
         ("allocate_nz", C.c_uint32), ("nwarps", C.c_uint32),
         ("min_nz", C.c_uint32), ("max_nz", C.c_uint32), ("nmax_per_thread", C.c_uint32),
+        ("variant", C.c_uint32),
         ("row_map", C.POINTER(C.c_int32)), ("row_map_inv", C.POINTER(C.c_int32)),
         ("reorder_rows", C.POINTER(C.c_uint32)), ("warp_offsets", C.POINTER(C.c_int32)),
         ("max_nz_rows", C.POINTER(C.c_uint32)), ("threads_per_row", C.POINTER(C.c_uint32)),
@@ -52,6 +53,7 @@ def lib():
         lp = C.POINTER(_Layout)
         L.wko_scan1.argtypes = [_i32p, C.c_uint32, C.c_uint32, lp]
         L.wko_scan2.argtypes = [_i32p, C.c_uint32, C.c_uint32, C.c_int32, lp]
+        L.wko_scan1_ablation.argtypes = [_i32p, C.c_uint32, C.c_uint32, C.c_int, lp]
         L.wko_free.argtypes = [lp]
         L.wko_process_f64.argtypes = [lp, _f64p, _i32p, _f64p, _i32p]
         L.wko_process_f32.argtypes = [lp, _f32p, _i32p, _f32p, _i32p]
@@ -130,13 +132,17 @@ def _wrap(c: _Layout) -> Layout:
 class OracleLayout:
     """Owns a C layout; use as a context manager or call free()."""
 
-    def __init__(self, rowptr, nz=None, kind=1, threshold=0):
+    def __init__(self, rowptr, nz=None, kind=1, threshold=0, ablation=0):
         rowptr = np.ascontiguousarray(rowptr, dtype=np.int32)
         nrows = len(rowptr) - 1
         nz = int(rowptr[-1]) if nz is None else int(nz)
         self.c = _Layout()
         L = lib()
-        if kind == 1:
+        if ablation:
+            if kind != 1:
+                raise ValueError("the ablation layouts are WPK1 layouts")
+            rc = L.wko_scan1_ablation(rowptr, nrows, nz, int(ablation), C.byref(self.c))
+        elif kind == 1:
             rc = L.wko_scan1(rowptr, nrows, nz, C.byref(self.c))
         else:
             rc = L.wko_scan2(rowptr, nrows, nz, int(threshold), C.byref(self.c))
@@ -321,6 +327,70 @@ class RefLib:
         rowptr = np.ascontiguousarray(rowptr, np.int32)
         h = self.L.ref_scan(rowptr, len(rowptr) - 1, int(rowptr[-1]), kind, int(threshold))
         return RefStructure(self.L, h, kind)
+
+
+class RefAblation:
+    """The reference's optimization.cu scans (scan, scan_nosort,
+    scan_nocoalesced, scan_nocoalesced_nosort) and warpKernel_nocoalesced,
+    compiled for the CPU by `make -C oracle ref` (oracle/_ref/libwkref_abl.so).
+    variant: 0 scan, 1 nosort, 2 nocoalesced, 3 both (the WKO_ABL_* flags)."""
+
+    PATH = os.path.join(HERE, "_ref", "libwkref_abl.so")
+
+    @staticmethod
+    def available():
+        return os.path.exists(RefAblation.PATH)
+
+    def __init__(self, rowptr, variant):
+        L = C.CDLL(self.PATH)
+        L.ref_abl_scan.restype = C.c_void_p
+        L.ref_abl_scan.argtypes = [_i32p, C.c_uint, C.c_uint, C.c_int]
+        L.ref_abl_info.argtypes = [C.c_void_p, _u32p]
+        L.ref_abl_field.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        L.ref_abl_free.argtypes = [C.c_void_p]
+        L.ref_abl_run_nocoalesced.argtypes = [C.c_void_p, _f64p, _i32p, _f64p, _f64p, C.c_int]
+        self.L = L
+        rowptr = np.ascontiguousarray(rowptr, np.int32)
+        self.nrows, self.nz = len(rowptr) - 1, int(rowptr[-1])
+        self.h = L.ref_abl_scan(rowptr, self.nrows, self.nz, int(variant))
+        info = np.zeros(2, np.uint32)
+        L.ref_abl_info(self.h, info)
+        self.nwarps, self.allocate_nz = int(info[0]), int(info[1])
+        sizes = [(np.int32, self.nrows), (np.int32, self.nrows), (np.uint32, self.nz),
+                 (np.int32, self.nwarps + 1), (np.uint32, self.nwarps)]
+        self.arrays = {}
+        for i, name in enumerate(FIELDS[:5]):
+            dt, cnt = sizes[i]
+            a = np.zeros(cnt, dt)
+            if cnt:
+                L.ref_abl_field(self.h, i, a.ctypes.data)
+            self.arrays[name] = a
+
+    def process(self, vals, cols):
+        pv = np.zeros(self.allocate_nz, np.float64)
+        pc = np.zeros(self.allocate_nz, np.int32)
+        rr = self.arrays["reorder_rows"]
+        pv[rr] = vals
+        pc[rr] = cols
+        return pv, pc
+
+    def run_nocoalesced(self, pvals, pcols, x, wpb=4):
+        y = np.zeros(self.nrows, np.float64)
+        self.L.ref_abl_run_nocoalesced(self.h, np.ascontiguousarray(pvals, np.float64),
+                                       np.ascontiguousarray(pcols, np.int32),
+                                       np.ascontiguousarray(x, np.float64), y, int(wpb))
+        return y
+
+    def free(self):
+        if self.h:
+            self.L.ref_abl_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 class RefStructure:

@@ -2,7 +2,8 @@
 
 The reference's host scan/process/reorder code (including
 reorder_columns_rowsort) and its WPK1 SpMV and assembly kernels
-(warpkernel.hpp) are compiled for the CPU by `make -C oracle ref` (needs the
+(warpkernel.hpp), and the ablation scans and warpKernel_nocoalesced of
+optimization.cu, are compiled for the CPU by `make -C oracle ref` (needs the
 reference sources) and run here on a fixed set of small matrices.  The
 fixture stores inputs and the reference's outputs, so tests on machines
 without the reference sources can still check the oracle and the CUDA path
@@ -108,6 +109,18 @@ def main():
                     data[f"{tag}/y_runx_{mode}"] = s2.run_wpk1(pv, pcr, xr, mapped=False)
                     s2.free()
             s.free()
+        # ablation layouts of optimization.cu, on matrices without empty rows
+        if n and np.all(np.diff(rp) > 0):
+            for va in (1, 2, 3):
+                tag = f"{name}/abl{va}"
+                A = O.RefAblation(rp, va)
+                data[f"{tag}/info"] = np.array([A.nwarps, A.allocate_nz], np.int64)
+                for f in O.FIELDS[:5]:
+                    data[f"{tag}/{f}"] = A.arrays[f]
+                if va & 2:
+                    pv, pc = A.process(v, c)
+                    data[f"{tag}/y"] = A.run_nocoalesced(pv, pc, x)
+                A.free()
     data["names"] = np.array(names)
     np.savez_compressed(OUT, **data)
     print(f"wrote {OUT} ({os.path.getsize(OUT)} bytes, {len(names)} matrices)")

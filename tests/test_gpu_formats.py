@@ -220,7 +220,7 @@ def test_layout_load_rejects_corrupt_files(tmp_path):
         "empty": b"",
     }
     # a row_map entry out of range: the first array follows the header
-    hdr = 8 + 4 + 9 * 4 + 8
+    hdr = 8 + 4 + 10 * 4 + 8  # magic, version, wk_layout_info, array length
     bad = bytearray(raw)
     bad[hdr:hdr + 4] = (10 ** 6).to_bytes(4, "little")
     cases["row_map"] = bytes(bad)

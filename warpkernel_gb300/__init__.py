@@ -6,5 +6,5 @@ warpkernel.hpp classes.
 """
 from .wpk import (WK_ORDER_EXACT, WK_ORDER_FAST, csr_matrix, engine, profiler,  # noqa: F401
                   read_matrix_market_file, stats, structure, structure2)
-from ._lib import WKError, load  # noqa: F401
+from ._lib import WK_ABL_NOCOALESCE, WK_ABL_NOSORT, WKError, load  # noqa: F401
 from . import fe  # noqa: F401

@@ -15,6 +15,7 @@ WK_OK = 0
 WK_F64, WK_F32, WK_BF16 = 0, 1, 2
 WK_WPK1, WK_WPK2 = 1, 2
 WK_ORDER_FAST, WK_ORDER_EXACT = 0, 1
+WK_ABL_NOSORT, WK_ABL_NOCOALESCE = 1, 2
 FIELDS = {
     "row_map": 0, "row_map_inv": 1, "reorder_rows": 2, "warp_offsets": 3,
     "max_nz_rows": 4, "threads_per_row": 5, "row_offset_warp": 6,
@@ -35,7 +36,7 @@ _szp = C.POINTER(C.c_size_t)
 class LayoutInfo(C.Structure):
     _fields_ = [("kind", C.c_int), ("nrows", u32), ("nznrows", u32), ("nz", u32),
                 ("allocate_nz", u32), ("nwarps", u32), ("min_nz", u32), ("max_nz", u32),
-                ("nmax_per_thread", u32)]
+                ("nmax_per_thread", u32), ("variant", u32)]
 
 
 class CGParams(C.Structure):
@@ -50,6 +51,7 @@ SIGNATURES = {
     "wk_debug_fail_alloc": (None, [C.c_int]),
     "wk_scan1": (C.c_int, [vp, u32, u32, vp, _pvp]),
     "wk_scan2": (C.c_int, [vp, u32, u32, i32, vp, _pvp]),
+    "wk_scan1_ablation": (C.c_int, [vp, u32, u32, C.c_int, vp, _pvp]),
     "wk_layout_info_get": (C.c_int, [vp, C.POINTER(LayoutInfo)]),
     "wk_layout_get": (C.c_int, [vp, C.c_int, vp, C.c_size_t, _szp]),
     "wk_layout_destroy": (C.c_int, [vp]),

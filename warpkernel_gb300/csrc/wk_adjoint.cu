@@ -452,6 +452,7 @@ extern "C" wk_status wk_adjoint_create(wk_engine *fwd, int kind, int32_t thresho
   if (!out) return set_error(WK_ERR_INVALID, "out is NULL");
   *out = nullptr;
   if (!fwd) return set_error(WK_ERR_INVALID, "engine is NULL");
+  WK_TRY(require_interleaved(fwd->layout, "wk_adjoint_create"));
   if (fwd->dtype != WK_F64 && fwd->dtype != WK_F32)
     return set_error(WK_ERR_INVALID, "the adjoint supports WK_F64 and WK_F32 engines");
   if (kind != WK_WPK1 && kind != WK_WPK2) return set_error(WK_ERR_INVALID, "kind must be WK_WPK1 or WK_WPK2");
@@ -511,7 +512,9 @@ extern "C" wk_status wk_adjoint_create(wk_engine *fwd, int kind, int32_t thresho
                                                          colsT.as<uint32_t>());
   if (cudaGetLastError() != cudaSuccess) return fail(set_error(WK_ERR_CUDA, "kernel launch failed"));
   // A^T's layout and engine (values in A^T's CSR order = A's values permuted)
-  s = make_layout(rowptrT.as<int32_t>(), m, nz, kind, threshold, st, &a->tl);
+  // a WPK1 adjoint keeps the forward layout's row order (sorted or CSR order)
+  s = make_layout(rowptrT.as<int32_t>(), m, nz, kind, threshold, st, &a->tl,
+                  kind == WK_WPK1 ? (int)L->info.variant : 0);
   if (s != WK_OK) return fail(s);
   if (eb == 8)
     k_gather_padded<unsigned long long><<<grid_for(nz, 256), 256, 0, st>>>(
@@ -531,7 +534,8 @@ extern "C" wk_status wk_adjoint_create(wk_engine *fwd, int kind, int32_t thresho
   s = make_engine(a->tl, fwd->dtype, valsc.p, colsT.as<int32_t>(), n, st, &a->te);
   if (s != WK_OK) return fail(s);
   // structurally symmetric with sorted rows: same row offsets and columns
-  if (m == n && kind == L->info.kind && (kind == WK_WPK1 || (uint32_t)threshold == L->info.nmax_per_thread)) {
+  if (m == n && kind == L->info.kind && a->tl->info.variant == L->info.variant &&
+      (kind == WK_WPK1 || (uint32_t)threshold == L->info.nmax_per_thread)) {
     if (cudaMemsetAsync(diff.p, 0, 4, st) != cudaSuccess) return fail(set_error(WK_ERR_CUDA, "memset failed"));
     k_count_diff<<<grid_for((size_t)n + 1, 256), 256, 0, st>>>(rowptrT.as<uint32_t>(), (const uint32_t *)L->d.rowptr,
                                                                (size_t)n + 1, diff.as<unsigned>());

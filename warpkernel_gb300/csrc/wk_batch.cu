@@ -219,6 +219,8 @@ extern "C" wk_status wk_batch_create(wk_engine *const *engines, const uint32_t *
   if (!out) return set_error(WK_ERR_INVALID, "out is NULL");
   *out = nullptr;
   if (!engines || !nrhs || count <= 0) return set_error(WK_ERR_INVALID, "empty batch");
+  for (int m = 0; m < count; m++)
+    if (engines[m]) WK_TRY(require_interleaved(engines[m]->layout, "wk_batch_create"));
   wk_batch *b = new (std::nothrow) wk_batch();
   if (!b) return set_error(WK_ERR_ALLOC, "host allocation failed");
   b->dtype = engines[0]->dtype;

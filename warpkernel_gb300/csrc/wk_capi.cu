@@ -95,7 +95,7 @@ wk_status check_square_cols(const wk_layout *l, const int32_t *dcols, cudaStream
 }
 
 wk_status scan_common(const int32_t *rowptr, uint32_t nrows, uint32_t nz, int kind, int32_t th,
-                      void *stream, wk_layout **out) {
+                      void *stream, wk_layout **out, int variant = 0) {
   if (!out) return set_error(WK_ERR_INVALID, "out is NULL");
   *out = nullptr;
   if (!rowptr) return set_error(WK_ERR_INVALID, "rowptr is NULL");
@@ -119,7 +119,7 @@ wk_status scan_common(const int32_t *rowptr, uint32_t nrows, uint32_t nz, int ki
     cudaError_t e = cudaMemcpyAsync(l->bufs[7].p, rowptr, ((size_t)nrows + 1) * 4, cudaMemcpyDefault, st);
     if (e != cudaSuccess) s = set_error(WK_ERR_CUDA, "rowptr copy failed: %s", cudaGetErrorString(e));
   }
-  if (s == WK_OK) s = build_layout(l, l->bufs[7].as<int32_t>(), kind, th, st);
+  if (s == WK_OK) s = build_layout(l, l->bufs[7].as<int32_t>(), kind, th, st, variant);
   if (s != WK_OK) {
     delete l;
     return s;
@@ -132,8 +132,14 @@ wk_status scan_common(const int32_t *rowptr, uint32_t nrows, uint32_t nz, int ki
 
 namespace wk {
 wk_status make_layout(const int32_t *d_rowptr, uint32_t nrows, uint32_t nz, int kind, int32_t threshold,
-                      cudaStream_t stream, wk_layout **out) {
-  return scan_common(d_rowptr, nrows, nz, kind, threshold, stream, out);
+                      cudaStream_t stream, wk_layout **out, int variant) {
+  return scan_common(d_rowptr, nrows, nz, kind, threshold, stream, out, variant);
+}
+
+wk_status require_interleaved(const wk_layout *l, const char *op) {
+  if (l && (l->info.variant & WK_ABL_NOCOALESCE))
+    return set_error(WK_ERR_INVALID, "%s does not accept a non-interleaved (WK_ABL_NOCOALESCE) layout", op);
+  return WK_OK;
 }
 }  // namespace wk
 
@@ -160,6 +166,15 @@ wk_status wk_scan1(const int32_t *rowptr, uint32_t nrows, uint32_t nz, void *str
 wk_status wk_scan2(const int32_t *rowptr, uint32_t nrows, uint32_t nz, int32_t threshold, void *stream,
                    wk_layout **out) {
   return scan_common(rowptr, nrows, nz, WK_WPK2, threshold, stream, out);
+}
+
+wk_status wk_scan1_ablation(const int32_t *rowptr, uint32_t nrows, uint32_t nz, int flags, void *stream,
+                            wk_layout **out) {
+  if (flags & ~(WK_ABL_NOSORT | WK_ABL_NOCOALESCE)) {
+    if (out) *out = nullptr;
+    return set_error(WK_ERR_INVALID, "unknown ablation flags %d", flags);
+  }
+  return scan_common(rowptr, nrows, nz, WK_WPK1, 0, stream, out, flags);
 }
 
 wk_status wk_layout_info_get(const wk_layout *l, wk_layout_info *info) {

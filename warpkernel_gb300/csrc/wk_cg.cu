@@ -280,6 +280,7 @@ using namespace wk;
 extern "C" wk_status wk_cg(wk_engine *e, const double *b, double *x, wk_cg_params *prm, void *stream) {
   if (!e || !b || !x || !prm) return set_error(WK_ERR_INVALID, "NULL argument");
   if (e->dtype != WK_F64) return set_error(WK_ERR_INVALID, "wk_cg needs a WK_F64 engine");
+  WK_TRY(require_interleaved(e->layout, "wk_cg"));
   WK_TRY(check_square(e));
   if (prm->max_iter <= 0) return set_error(WK_ERR_INVALID, "max_iter must be positive");
   cudaStream_t st = (cudaStream_t)stream;
@@ -328,6 +329,8 @@ extern "C" wk_status wk_cg(wk_engine *e, const double *b, double *x, wk_cg_param
 extern "C" wk_status wk_ir_cg(wk_engine *e64, wk_engine *lo, const double *b, double *x, wk_cg_params *prm,
                               void *stream) {
   if (!e64 || !lo || !b || !x || !prm) return set_error(WK_ERR_INVALID, "NULL argument");
+  WK_TRY(require_interleaved(e64->layout, "wk_ir_cg"));
+  WK_TRY(require_interleaved(lo->layout, "wk_ir_cg"));
   if (e64->dtype != WK_F64) return set_error(WK_ERR_INVALID, "wk_ir_cg: the residual engine must be WK_F64");
   if (lo->dtype != WK_F32 && lo->dtype != WK_BF16)
     return set_error(WK_ERR_INVALID, "wk_ir_cg: the inner engine must be WK_F32 or WK_BF16");

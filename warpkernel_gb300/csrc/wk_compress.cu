@@ -134,5 +134,6 @@ using namespace wk;
 
 extern "C" wk_status wk_engine_compress_cols(wk_engine *e, void *stream, uint32_t *wide_warps) {
   if (!e) return set_error(WK_ERR_INVALID, "engine is NULL");
+  WK_TRY(require_interleaved(e->layout, "wk_engine_compress_cols"));
   return build_compressed_cols(e, (cudaStream_t)stream, wide_warps);
 }

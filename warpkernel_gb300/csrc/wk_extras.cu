@@ -217,6 +217,7 @@ using namespace wk;
 extern "C" wk_status wk_run_assembly(wk_engine *e, int nblocks, int blocksize, void *dy, void *stream,
                                      float *seconds) {
   if (!e || !dy) return set_error(WK_ERR_INVALID, "NULL argument");
+  WK_TRY(require_interleaved(e->layout, "wk_run_assembly"));
   const wk_layout *l = e->layout;
   unsigned grid, block;
   WK_TRY(launch_shape(l->info.nwarps, nblocks, blocksize, &grid, &block));
@@ -337,6 +338,7 @@ extern "C" wk_status wk_layout_load(const char *path, void *stream, wk_layout **
   wk_layout_info I;
   if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kMagic, 8) != 0 || std::fread(&version, 4, 1, f) != 1 ||
       version != 1 || std::fread(&I, sizeof I, 1, f) != 1 || (I.kind != WK_WPK1 && I.kind != WK_WPK2) ||
+      I.variant > (WK_ABL_NOSORT | WK_ABL_NOCOALESCE) || (I.variant && I.kind != WK_WPK1) ||
       I.nrows > 0x7fffffffu || I.nz > 0x7fffffffu || I.nwarps > 0x7fffffffu || I.allocate_nz > 0x7fffffffu) {
     std::fclose(f);
     return set_error(WK_ERR_INVALID, "%s is not a WPK layout file", path);
@@ -352,11 +354,11 @@ extern "C" wk_status wk_layout_load(const char *path, void *stream, wk_layout **
   if (!ok) return set_error(WK_ERR_INVALID, "%s: truncated or inconsistent arrays", path);
   wk_layout *l = nullptr;
   WK_TRY(make_layout(rp.data(), I.nrows, I.nz, I.kind, k2 ? (int32_t)I.nmax_per_thread : 0,
-                     (cudaStream_t)stream, &l));
+                     (cudaStream_t)stream, &l, (int)I.variant));
   const wk_layout_info &B = l->info;
   ok = B.kind == I.kind && B.nrows == I.nrows && B.nznrows == I.nznrows && B.nz == I.nz &&
        B.allocate_nz == I.allocate_nz && B.nwarps == I.nwarps && B.min_nz == I.min_nz && B.max_nz == I.max_nz &&
-       B.nmax_per_thread == I.nmax_per_thread;
+       B.nmax_per_thread == I.nmax_per_thread && B.variant == I.variant;
   auto same = [&](const void *dev, const void *host, size_t bytes) {
     if (!ok || !bytes) return;
     std::vector<char> h(bytes);

@@ -140,7 +140,7 @@ namespace wk {
 // ---- launchers (stream-ordered) ----------------------------------------------------
 // Builds all layout arrays from a device CSR row-pointer array (kind 1/2).
 wk_status build_layout(wk_layout *l, const int32_t *d_rowptr, int kind, int32_t threshold,
-                       cudaStream_t stream);
+                       cudaStream_t stream, int variant = 0);
 // Padded gather of values (elem bytes 8/4/2) and column indices; cols are
 // optionally renumbered through row_map_inv.  Either output may be null.
 wk_status launch_process(const wk_layout *l, const void *vals, int elem_bytes,
@@ -166,7 +166,10 @@ wk_status radix_sort_pairs(uint32_t *k0, uint32_t *k1, uint32_t *v0, uint32_t *v
 // Allocates a layout and builds it on the device from a device copy of the
 // CSR row offsets (the layout keeps its own copy).
 wk_status make_layout(const int32_t *d_rowptr, uint32_t nrows, uint32_t nz, int kind, int32_t threshold,
-                      cudaStream_t stream, wk_layout **out);
+                      cudaStream_t stream, wk_layout **out, int variant = 0);
+// WK_ERR_INVALID for layouts whose slots are not interleaved (WK_ABL_NOCOALESCE),
+// which only the plain SpMV and data-movement calls accept; `op` names the call.
+wk_status require_interleaved(const wk_layout *l, const char *op);
 // Allocates an engine over layout l (takes a layout reference) from device
 // CSR-ordered values (elem bytes 8/4/2) and column indices.
 wk_status make_engine(wk_layout *l, int dtype, const void *d_vals, const int32_t *d_cols, uint32_t ncols,

@@ -157,11 +157,13 @@ __global__ void k_rowlen(const int32_t *__restrict__ rowptr, uint32_t n, uint32_
   }
 }
 
+// Sort keys: length descending (maxlen - len), or for the unsorted ablation
+// layout only "empty rows last" (len == 0), so rows keep their CSR order.
 __global__ void k_init_keys(const uint32_t *__restrict__ len, uint32_t n, uint32_t maxlen,
-                            uint32_t *__restrict__ keys, uint32_t *__restrict__ vals) {
+                            uint32_t *__restrict__ keys, uint32_t *__restrict__ vals, int nosort) {
   for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
        r += (size_t)gridDim.x * blockDim.x) {
-    keys[r] = maxlen - len[r];
+    keys[r] = nosort ? (uint32_t)(len[r] == 0) : maxlen - len[r];
     vals[r] = (uint32_t)r;
   }
 }
@@ -222,15 +224,15 @@ __global__ void __launch_bounds__(RS_WARPS * 32)
 }
 
 // row_map[p] (already in `vals`), slen[p], row_map_inv[row_map[p]] = p.
-__global__ void k_finish_sort(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
-                              uint32_t n, uint32_t maxlen, int32_t *__restrict__ row_map,
-                              int32_t *__restrict__ row_map_inv, uint32_t *__restrict__ slen) {
+__global__ void k_finish_sort(const uint32_t *__restrict__ vals, const uint32_t *__restrict__ len, uint32_t n,
+                              int32_t *__restrict__ row_map, int32_t *__restrict__ row_map_inv,
+                              uint32_t *__restrict__ slen) {
   for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < n;
        p += (size_t)gridDim.x * blockDim.x) {
     uint32_t r = vals[p];
     row_map[p] = (int32_t)r;
     row_map_inv[r] = (int32_t)p;
-    slen[p] = maxlen - keys[p];
+    slen[p] = len[r];
   }
 }
 
@@ -271,13 +273,15 @@ __device__ __forceinline__ WarpSplit split_rule(uint32_t A, uint32_t cnt, uint32
 }
 
 __global__ void k_warp_split(const uint32_t *__restrict__ slen, uint32_t nzr, uint32_t W0,
-                             uint32_t th, int wpk2, WarpSplit *__restrict__ ws,
+                             uint32_t th, int wpk2, int nosort, WarpSplit *__restrict__ ws,
                              unsigned long long *__restrict__ count,
                              unsigned long long *__restrict__ slots) {
   for (size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x; w < W0;
        w += (size_t)gridDim.x * blockDim.x) {
     uint32_t A = slen[w * WS];  // sorted descending: the warp's first row is its longest
     uint32_t cnt = min((uint32_t)WS, nzr - (uint32_t)w * WS);
+    if (nosort)
+      for (uint32_t q = 1; q < cnt; q++) A = max(A, slen[w * WS + q]);
     WarpSplit s = split_rule(A, cnt, th, wpk2 != 0);
     ws[w] = s;
     unsigned long long c = s.full ? s.tpr : 1u;
@@ -322,7 +326,7 @@ __global__ void k_reorder_rows(const WarpSplit *__restrict__ ws,
                                const unsigned long long *__restrict__ soff,
                                const int32_t *__restrict__ row_map, const uint32_t *__restrict__ slen,
                                const int32_t *__restrict__ rowptr, uint32_t nzr,
-                               uint32_t *__restrict__ reorder_rows) {
+                               uint32_t *__restrict__ reorder_rows, int nocoal) {
   for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < nzr;
        p += (size_t)gridDim.x * blockDim.x) {
     size_t w = p / WS;
@@ -336,6 +340,10 @@ __global__ void k_reorder_rows(const WarpSplit *__restrict__ ws,
     uint32_t base = (uint32_t)(soff[w] + (unsigned long long)j * WS * s.steps);
     uint32_t len = slen[p];
     uint32_t k0 = (uint32_t)rowptr[row_map[p]];
+    if (nocoal) {  // WPK1 lane r holds its row's entries contiguously
+      for (uint32_t e = 0; e < len; e++) reorder_rows[k0 + e] = base + r * s.steps + e;
+      continue;
+    }
     uint32_t lane0 = base + r * s.tpr;
     for (uint32_t e = 0; e < len; e++)
       reorder_rows[k0 + e] = lane0 + e / s.steps + WS * (e % s.steps);
@@ -350,7 +358,7 @@ __global__ void k_process(const int4 *__restrict__ desc, uint32_t W, const int32
                           const int32_t *__restrict__ row_map_inv, const uint32_t *__restrict__ slen,
                           const int32_t *__restrict__ rowptr, uint32_t nzr, const E *__restrict__ vals,
                           const int32_t *__restrict__ cols, E *__restrict__ pv, int32_t *__restrict__ pc,
-                          int renumber) {
+                          int renumber, int nocoal) {
   const int lane = threadIdx.x & 31;
   for (size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS; w < W;
        w += (size_t)gridDim.x * blockDim.x / WS) {
@@ -365,8 +373,10 @@ __global__ void k_process(const int4 *__restrict__ desc, uint32_t W, const int32
       k0 = (uint32_t)rowptr[row_map[p]];
     }
     const uint32_t A = (uint32_t)d.y;
-    size_t slot = (size_t)(uint32_t)d.x + lane;
-    for (uint32_t i = 0; i < A; i++, slot += WS) {
+    // interleaved: slot o + lane + 32 i; non-interleaved ablation: o + lane * A + i
+    size_t slot = (size_t)(uint32_t)d.x + (nocoal ? (size_t)lane * A : (size_t)lane);
+    const size_t stride = nocoal ? 1 : WS;
+    for (uint32_t i = 0; i < A; i++, slot += stride) {
       uint32_t e = i + t * A;
       E v = E(0);
       int32_t c = 0;
@@ -447,10 +457,13 @@ wk_status scan_u32(const uint32_t *in, uint32_t *out, size_t n, uint32_t *d_tota
 }
 
 wk_status build_layout(wk_layout *l, const int32_t *d_rowptr, int kind, int32_t threshold,
-                       cudaStream_t st) {
+                       cudaStream_t st, int variant) {
   const uint32_t n = l->info.nrows, nz = l->info.nz;
   const bool wpk2 = kind == WK_WPK2;
+  if (wpk2 && variant) return set_error(WK_ERR_INVALID, "the ablation layouts are WPK1 layouts");
+  const int nosort = (variant & WK_ABL_NOSORT) ? 1 : 0, nocoal = (variant & WK_ABL_NOCOALESCE) ? 1 : 0;
   l->info.kind = kind;
+  l->info.variant = (uint32_t)variant;
   l->info.nmax_per_thread = wpk2 ? (uint32_t)threshold : 0u;
 
   // 1. lengths, checks
@@ -477,10 +490,11 @@ wk_status build_layout(wk_layout *l, const int32_t *d_rowptr, int kind, int32_t 
     WK_TRY(vb[i].alloc((size_t)n * 4));
   }
   k_init_keys<<<grid_for(n, 256), 256, 0, st>>>(len.as<uint32_t>(), n, maxlen, kb[0].as<uint32_t>(),
-                                                vb[0].as<uint32_t>());
+                                                vb[0].as<uint32_t>(), nosort);
   WK_CHECK_LAUNCH();
   int bits = 0;
   while (bits < 32 && (maxlen >> bits)) bits++;
+  if (nosort) bits = 1;
   int cur = 0;
   WK_TRY(radix_sort_pairs(kb[0].as<uint32_t>(), kb[1].as<uint32_t>(), vb[0].as<uint32_t>(), vb[1].as<uint32_t>(), n,
                           bits, st, &cur));
@@ -492,8 +506,8 @@ wk_status build_layout(wk_layout *l, const int32_t *d_rowptr, int kind, int32_t 
   d.row_map_inv = l->bufs[1].as<int32_t>();
   d.slen = l->bufs[8].as<uint32_t>();
   d.rowptr = const_cast<int32_t *>(d_rowptr);
-  k_finish_sort<<<grid_for(n, 256), 256, 0, st>>>(kb[cur].as<uint32_t>(), vb[cur].as<uint32_t>(), n,
-                                                  maxlen, d.row_map, d.row_map_inv, d.slen);
+  k_finish_sort<<<grid_for(n, 256), 256, 0, st>>>(vb[cur].as<uint32_t>(), len.as<uint32_t>(), n, d.row_map,
+                                                  d.row_map_inv, d.slen);
   WK_CHECK_LAUNCH();
 
   // 4. warp tables
@@ -505,7 +519,7 @@ wk_status build_layout(wk_layout *l, const int32_t *d_rowptr, int kind, int32_t 
   WK_TRY(tot.alloc(2 * 8));
   auto *totals = tot.as<unsigned long long>();
   if (W0) {
-    k_warp_split<<<grid_for(W0, 256), 256, 0, st>>>(d.slen, nzr, W0, (uint32_t)threshold, wpk2,
+    k_warp_split<<<grid_for(W0, 256), 256, 0, st>>>(d.slen, nzr, W0, (uint32_t)threshold, wpk2, nosort,
                                                     wsb.as<WarpSplit>(), cnt.as<unsigned long long>(),
                                                     slots.as<unsigned long long>());
     WK_CHECK_LAUNCH();
@@ -561,7 +575,7 @@ wk_status build_layout(wk_layout *l, const int32_t *d_rowptr, int kind, int32_t 
   d.reorder_rows = l->bufs[2].as<uint32_t>();
   if (nzr) {
     k_reorder_rows<<<grid_for(nzr, 256), 256, 0, st>>>(wsb.as<WarpSplit>(), slots.as<unsigned long long>(),
-                                                       d.row_map, d.slen, d_rowptr, nzr, d.reorder_rows);
+                                                       d.row_map, d.slen, d_rowptr, nzr, d.reorder_rows, nocoal);
     WK_CHECK_LAUNCH();
   }
   WK_CUDA(cudaStreamSynchronize(st));  // temporaries are freed on return
@@ -577,7 +591,7 @@ wk_status launch_process(const wk_layout *l, const void *vals, int elem_bytes, c
 #define WK_PROCESS(E)                                                                          \
   k_process<E><<<grid, 256, 0, st>>>(d.warp_desc, W, d.row_map, d.row_map_inv, d.slen, d.rowptr, \
                                      l->info.nznrows, (const E *)vals, cols, (E *)pvals, pcols,   \
-                                     renumber ? 1 : 0)
+                                     renumber ? 1 : 0, (l->info.variant & WK_ABL_NOCOALESCE) ? 1 : 0)
   switch (elem_bytes) {
     case 8: WK_PROCESS(unsigned long long); break;
     case 4: WK_PROCESS(uint32_t); break;

@@ -141,6 +141,7 @@ extern "C" wk_status wk_residual_static(wk_engine *e, const double *x, const dou
                                         double *norm2, void *stream) {
   if (!e || !x || !b || !r) return set_error(WK_ERR_INVALID, "NULL argument");
   if (e->dtype != WK_F64) return set_error(WK_ERR_INVALID, "wk_residual_static needs a WK_F64 engine");
+  WK_TRY(require_interleaved(e->layout, "wk_residual_static"));
   const unsigned grid = residual_grid(e->layout);
   if (grid > kResidualStaticBlocks)
     return set_error(WK_ERR_INVALID,
@@ -156,6 +157,7 @@ extern "C" wk_status wk_residual(wk_engine *e, const double *x, const double *b,
                                  void *stream) {
   if (!e || !x || !b || !r) return set_error(WK_ERR_INVALID, "NULL argument");
   if (e->dtype != WK_F64) return set_error(WK_ERR_INVALID, "wk_residual needs a WK_F64 engine");
+  WK_TRY(require_interleaved(e->layout, "wk_residual"));
   cudaStream_t st = (cudaStream_t)stream;
   const unsigned grid = residual_grid(e->layout);
   if (e->scratch.bytes < (size_t)grid * sizeof(double)) WK_TRY(e->scratch.alloc((size_t)grid * sizeof(double)));

@@ -58,6 +58,30 @@ __global__ void __launch_bounds__(1024) k_spmv_fast(const V *__restrict__ pv, co
   if (p < nzr && (lane & (T - 1)) == 0) store_row<typename Tr<V>::Acc, MAPPED>(y, row_map, p, s);
 }
 
+// warpKernel_nocoalesced (optimization.cu:91-114) for the non-interleaved
+// ablation layout: lane l of a WPK1 warp owns slots o + l * A ... o + l * A +
+// A - 1 and sums them in order (first product, then fma).  Neighbouring lanes
+// read addresses A slots apart, so a warp load touches up to 32 sectors.
+template <typename V, typename X, bool MAPPED, bool L1>
+__global__ void __launch_bounds__(1024) k_spmv_nocoal(const V *__restrict__ pv, const int32_t *__restrict__ pc,
+                                                      const int4 *__restrict__ desc, uint32_t W,
+                                                      const int32_t *__restrict__ row_map, uint32_t nzr,
+                                                      const X *__restrict__ x, typename Tr<V>::Acc *__restrict__ y) {
+  typedef typename Tr<V>::Acc Acc;
+  const uint32_t lane = threadIdx.x & 31;
+  const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
+  if (w >= W) return;
+  const int4 d = desc[w];
+  const uint32_t p = (uint32_t)d.w + lane;
+  if (p >= nzr) return;
+  const uint32_t A = (uint32_t)d.y;
+  const size_t o = (size_t)(uint32_t)d.x + (size_t)lane * A;
+  Acc s = Tr<V>::acc(pv[o]) * (Acc)Tr<X>::acc(gather<L1>(x, pc[o]));
+  for (uint32_t i = 1; i < A; i++)
+    s = fma_acc(Tr<V>::acc(pv[o + i]), (Acc)Tr<X>::acc(gather<L1>(x, pc[o + i])), s);
+  store_row<Acc, MAPPED>(y, row_map, p, s);
+}
+
 // Fast order with the 16-bit column storage of wk_engine_compress_cols.
 template <typename V, typename X, bool MAPPED, bool L1>
 __global__ void __launch_bounds__(1024) k_spmv_fast_c(const V *__restrict__ pv, const uint16_t *__restrict__ c16,
@@ -91,6 +115,15 @@ wk_status dispatch(const RunArgs &a, unsigned grid, unsigned block) {
   const uint32_t W = l->info.nwarps, nzr = l->info.nznrows;
 #define WK_LAUNCH(K, M, C) K<V, X, M, C><<<grid, block, 0, a.stream>>>(pv, pc, desc, W, rm, nzr, x, y)
   const bool c = a.cache != 0;
+  if (l->info.variant & WK_ABL_NOCOALESCE) {  // one order only: the reference's
+    if (a.mapped) {
+      if (c) WK_LAUNCH(k_spmv_nocoal, true, true); else WK_LAUNCH(k_spmv_nocoal, true, false);
+    } else {
+      if (c) WK_LAUNCH(k_spmv_nocoal, false, true); else WK_LAUNCH(k_spmv_nocoal, false, false);
+    }
+    WK_CHECK_LAUNCH();
+    return WK_OK;
+  }
   if (e->compressed && a.order == WK_ORDER_FAST) {
     const uint16_t *c16 = e->c16.as<uint16_t>();
     const int32_t *c32 = e->c32.as<int32_t>();

@@ -87,6 +87,23 @@ class structure:
         self._set(h)
         return self
 
+    def scan_ablation(self, nz, nrows, rows, flags, stream=None):
+        """The WPK1 ablation layouts of optimization.cu: flags WK_ABL_NOSORT
+        (scan_nosort, rows in CSR order), WK_ABL_NOCOALESCE (scan_nocoalesced,
+        each lane's entries contiguous) or both (scan_nocoalesced_nosort)."""
+        if self.kind != WK_WPK1:
+            raise ValueError("the ablation layouts are WPK1 layouts")
+        if isinstance(rows, np.ndarray):
+            rows = np.ascontiguousarray(rows, dtype=np.int32)
+        self._release()
+        h = C.c_void_p()
+        check(load().wk_scan1_ablation(_ptr(rows), int(nrows), int(nz), int(flags), _stream_ptr(stream),
+                                       C.byref(h)))
+        self._set(h)
+        return self
+
+    variant = property(lambda s: s._info.variant)
+
     def _set(self, h):
         self._h = h
         info = LayoutInfo()
