@@ -296,9 +296,9 @@ def _event_ms(fn, reps, warm=3):
 
 
 def suite_mixed_and_cg(reps):
-    """hex 96^3 (3 dof, seed 2): fp64 vs FP32 / BF16-stored SpMV with FP32
-    accumulation (error vs the fp64 host CSR product), then fp64 CG vs
-    iterative-refinement CG to 1e-10 with b = A x*."""
+    """hex 96^3 (3 dof, seed 2): fp64 vs FP32 / BF16 / scaled-FP16 (WK_F16S)
+    stored SpMV with FP32 accumulation (error vs the fp64 host CSR product),
+    then fp64 CG vs iterative-refinement CG to 1e-10 with b = A x*."""
     import numpy as np
     import torch
 
@@ -319,7 +319,9 @@ def suite_mixed_and_cg(reps):
                            "gbs": round((12 * nnz + 20 * n) / ms64 / 1e6, 1),
                            "rel_err": float(np.linalg.norm(y64.cpu().numpy() - y_ref) / np.linalg.norm(y_ref))}
     engines = {}
-    for name, tdt, dt, vb in (("f32", torch.float32, "f32", 4), ("bf16", torch.bfloat16, "bf16", 2)):
+    # (name, value/x tensor type, engine dtype, stored value bytes, x bytes)
+    for name, tdt, dt, vb, xb in (("f32", torch.float32, "f32", 4, 4), ("bf16", torch.bfloat16, "bf16", 2, 2),
+                                  ("f16s", torch.float32, "f16s", 2, 4)):
         e = wk.engine(k, fe.convert(vals, tdt), cols, dtype=dt)
         xd = fe.convert(x, tdt)
         yd = torch.zeros(n, dtype=torch.float32, device="cuda")
@@ -331,7 +333,7 @@ def suite_mixed_and_cg(reps):
             ib = 2 if comp else 4
             res["paths"][name + ("+cols16" if comp else "")] = {
                 "ms": round(ms, 4), "gnnz_s": round(nnz / ms / 1e6, 1), "speedup": round((nnz / ms) / base, 3),
-                "gbs": round(((vb + ib) * nnz + (vb + 4 + 4) * n) / ms / 1e6, 1), "rel_err": err}
+                "gbs": round(((vb + ib) * nnz + (xb + 4 + 4) * n) / ms / 1e6, 1), "rel_err": err}
         engines[name] = e
     # CG: b = A x*, x* uniform(-1, 1)
     xs = fe.uniform_vec(2, 1, n)
@@ -344,9 +346,12 @@ def suite_mixed_and_cg(reps):
     ir = wk.wpk.ir_cg(e64, engines["f32"], b, xi, tol=1e-10, inner_tol=1e-5, max_inner=20000, check_every=16)
     xb = torch.zeros_like(b)
     irb = wk.wpk.ir_cg(e64, engines["bf16"], b, xb, tol=1e-10, inner_tol=1e-2, max_inner=20000, check_every=16)
-    res["cg"] = {"fp64_cg": cg, "ir_cg_f32_inner": ir, "ir_cg_bf16_inner": irb,
+    xh = torch.zeros_like(b)
+    irh = wk.wpk.ir_cg(e64, engines["f16s"], b, xh, tol=1e-10, inner_tol=1e-3, max_inner=20000, check_every=16)
+    res["cg"] = {"fp64_cg": cg, "ir_cg_f32_inner": ir, "ir_cg_bf16_inner": irb, "ir_cg_f16s_inner": irh,
                  "ir_f32_speedup": round(cg["seconds"] / ir["seconds"], 3),
-                 "ir_bf16_speedup": round(cg["seconds"] / irb["seconds"], 3)}
+                 "ir_bf16_speedup": round(cg["seconds"] / irb["seconds"], 3),
+                 "ir_f16s_speedup": round(cg["seconds"] / irh["seconds"], 3)}
     return res
 
 

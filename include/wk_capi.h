@@ -45,8 +45,13 @@ enum {
 typedef struct wk_layout wk_layout; /* a scanned WPK1/WPK2 layout (device resident) */
 typedef struct wk_engine wk_engine; /* padded values + column indices on the device */
 
-/* Element types of values and vectors. */
-enum { WK_F64 = 0, WK_F32 = 1, WK_BF16 = 2 };
+/* Element types of values and vectors.  WK_F16S (no reference counterpart):
+ * values stored as FP16 relative to a power-of-two scale per layout warp (the
+ * warp's largest magnitude maps into [2^14, 2^15)), 2 bytes per value like
+ * WK_BF16 but with FP16's 11-bit significand; callers pass FP32 values and
+ * FP32 x, and get FP32 y (FP32 accumulation, the row total multiplied by the
+ * scale, which is exact). */
+enum { WK_F64 = 0, WK_F32 = 1, WK_BF16 = 2, WK_F16S = 3 };
 
 /* Layout kinds: WPK1 = structure, WPK2 = structure2. */
 enum { WK_WPK1 = 1, WK_WPK2 = 2 };

@@ -1,0 +1,121 @@
+"""WK_F16S storage: FP16 values relative to a power-of-two scale per layout
+warp.  The stored values decode exactly to the emulation below, the SpMV
+matches the FP64 product of the decoded values to FP32 accumulation accuracy,
+and the storage error on a finite-element matrix stays under the 1e-3 bar
+that BF16 storage misses."""
+import numpy as np
+import pytest
+
+from conftest import random_csr
+from oracle import wk_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def wk():
+    import warpkernel_gb300
+    return warpkernel_gb300
+
+
+def torch():
+    import torch as t
+    return t
+
+
+def emulate_f16s(L, vals, cols):
+    """Per layout warp: scale 2^(k-15) from the largest magnitude m = f 2^k,
+    values / scale rounded to FP16 (nearest even), decoded as FP32 * scale."""
+    lay = L.layout
+    pv, _ = L.process(vals.astype(np.float32).astype(np.float64), cols)
+    pv = pv.astype(np.float32)
+    out = np.zeros_like(pv)
+    wo, mx = lay.arrays["warp_offsets"], lay.arrays["max_nz_rows"]
+    for w in range(lay.nwarps):
+        a, b = int(wo[w]), int(wo[w]) + 32 * int(mx[w])
+        seg = pv[a:b]
+        m = float(np.max(np.abs(seg))) if b > a else 0.0
+        e = 0
+        if m > 0 and np.isfinite(m):
+            e = max(int(np.frexp(np.float32(m))[1]) - 15, -126)
+        sc, inv = np.float32(np.ldexp(1.0, e)), np.float32(np.ldexp(1.0, -e))
+        h = (seg * inv).astype(np.float16)
+        out[a:b] = h.astype(np.float32) * sc
+    return out
+
+
+def make(kind, rp, cols, vals, th, dtype):
+    k = wk().structure() if kind == 1 else wk().structure2()
+    if kind == 1:
+        k.scan(len(cols), len(rp) - 1, None, rp)
+    else:
+        k.scan(len(cols), len(rp) - 1, None, rp, None, th)
+    return k, wk().engine(k, vals.astype(np.float32), cols, dtype=dtype)
+
+
+@pytest.mark.parametrize("kind,th", [(1, 0), (2, 5)])
+def test_f16s_values_decode_to_the_emulation(kind, th):
+    rng = np.random.default_rng(kind + th)
+    rp, cols, vals = random_csr(rng, 3000, 60, p_empty=0.1)
+    vals = vals * np.exp(rng.uniform(-20, 20, len(vals)))  # magnitudes over ~17 decades
+    k, eng = make(kind, rp, cols, vals, th, "f16s")
+    with O.OracleLayout(rp, kind=kind, threshold=th) as L:
+        ref = emulate_f16s(L, vals, cols)
+    np.testing.assert_array_equal(eng.device_values.view(np.uint32), ref.view(np.uint32))
+
+
+@pytest.mark.parametrize("kind,th", [(1, 0), (2, 5), (2, 81)])
+def test_f16s_spmv_accuracy_and_paths(kind, th):
+    t = torch()
+    rp, cols, vals = O.fe_matrix(3, 14, 13, 12, 3, value_mode=1, seed=2)
+    n = len(rp) - 1
+    x = O.uniform_vec(2, 0, n)
+    x32 = x.astype(np.float32)
+    k, eng = make(kind, rp, cols, vals, th, "f16s")
+    dec = eng.device_values.astype(np.float64)
+    with O.OracleLayout(rp, kind=kind, threshold=th) as L:
+        y_dec = L.run(dec, L.process(vals, cols)[1], x32.astype(np.float64))  # FP64 product of the stored values
+    y64 = O.csr_spmv(rp, cols, vals, x)
+    dx = t.from_numpy(x32).cuda()
+    ys = {}
+    for order in (0, 1):
+        for cache in (True, False):
+            dy = t.zeros(n, dtype=t.float32, device="cuda")
+            eng.run(0, 128, dx, dy, cache=cache, order=order)
+            ys[(order, cache)] = dy.cpu().numpy().astype(np.float64)
+            rel_acc = np.linalg.norm(ys[(order, cache)] - y_dec) / np.linalg.norm(y_dec)
+            assert rel_acc < 1e-6, rel_acc  # FP32 accumulation of the stored values
+    rel_storage = np.linalg.norm(ys[(0, True)] - y64) / np.linalg.norm(y64)
+    assert rel_storage < 1e-3, rel_storage  # the storage bar BF16 misses (~2.3e-3)
+    # 16-bit columns: bit-identical to the fast order
+    eng.compress_cols()
+    dy = t.zeros(n, dtype=t.float32, device="cuda")
+    eng.run(0, 128, dx, dy, order=0)
+    np.testing.assert_array_equal(dy.cpu().numpy(), ys[(0, True)].astype(np.float32))
+    # host vectors
+    yh = t.zeros(n, dtype=t.float32)
+    eng.run_host(t.from_numpy(x32), yh)
+    np.testing.assert_array_equal(yh.numpy(), ys[(0, True)].astype(np.float32))
+    # assembly: row sums of the stored values
+    ds = t.zeros(n, dtype=t.float32, device="cuda")
+    eng.run_assembly(0, 0, ds)
+    with O.OracleLayout(rp, kind=kind, threshold=th) as L:
+        sums = L.assembly(dec)
+    assert np.max(np.abs(ds.cpu().numpy() - sums)) <= 1e-6 * np.max(np.abs(sums))
+
+
+def test_f16s_set_values_and_ir_cg():
+    t = torch()
+    rp, cols, vals = O.fe_matrix(3, 12, 12, 12, 3, value_mode=1, seed=2)
+    n = len(rp) - 1
+    k = wk().structure2().scan(len(cols), n, None, rp, None, 81)
+    e64 = wk().engine(k, vals, cols)
+    lo = wk().engine(k, np.zeros(len(cols), np.float32), cols, dtype="f16s")
+    lo.set_values(vals.astype(np.float32))
+    lo2 = wk().engine(k, vals.astype(np.float32), cols, dtype="f16s")
+    np.testing.assert_array_equal(lo.device_values, lo2.device_values)
+    xs = O.uniform_vec(5, 0, n)
+    b = t.from_numpy(O.csr_spmv(rp, cols, vals, xs)).cuda()
+    x = t.zeros(n, dtype=t.float64, device="cuda")
+    res = wk().wpk.ir_cg(e64, lo, b, x, tol=1e-10)
+    assert res["converged"] and res["relres"] <= 1e-10
+    assert np.linalg.norm(x.cpu().numpy() - xs) / np.linalg.norm(xs) < 1e-6

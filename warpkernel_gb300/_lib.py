@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libwarpkernel_gb300.so")
 
 WK_OK = 0
-WK_F64, WK_F32, WK_BF16 = 0, 1, 2
+WK_F64, WK_F32, WK_BF16, WK_F16S = 0, 1, 2, 3
 WK_WPK1, WK_WPK2 = 1, 2
 WK_ORDER_FAST, WK_ORDER_EXACT = 0, 1
 WK_ABL_NOSORT, WK_ABL_NOCOALESCE = 1, 2

@@ -59,9 +59,12 @@ size_t dtype_size(int dtype) {
     case WK_F64: return 8;
     case WK_F32: return 4;
     case WK_BF16: return 2;
+    case WK_F16S: return 4;
   }
   return 0;
 }
+
+size_t stored_size(int dtype) { return dtype == WK_F16S ? 2 : dtype_size(dtype); }
 
 }  // namespace wk
 
@@ -296,16 +299,19 @@ wk_status wk_engine_create(wk_layout *l, int dtype, const void *vals, const int3
   DevView v, c;
   if (s == WK_OK) s = v.from(vals, nz * eb, st);
   if (s == WK_OK) s = c.from(cols, nz * 4, st);
-  if (s == WK_OK) s = e->vals.alloc(anz * eb);
+  if (s == WK_OK) s = e->vals.alloc(anz * stored_size(dtype));
   if (s == WK_OK) s = e->cols.alloc(anz * 4);
   if (s == WK_OK) s = e->status.alloc(64);
+  if (s == WK_OK && dtype == WK_F16S) s = e->scale.alloc((size_t)l->info.nwarps * 4);
   int bad = 0;
   if (s == WK_OK) {
     cudaMemsetAsync(e->status.p, 0, 64, st);
     s = launch_check_cols((const int32_t *)c.dptr, nz, ncols, e->status.as<int>(), st);
   }
-  if (s == WK_OK) s = launch_process(l, v.dptr, (int)eb, (const int32_t *)c.dptr, e->vals.p,
+  e->layout = l;  // not yet referenced: cleared again on failure
+  if (s == WK_OK) s = launch_process(l, nullptr, (int)eb, (const int32_t *)c.dptr, nullptr,
                                      e->cols.as<int32_t>(), false, st);
+  if (s == WK_OK) s = load_values(e, v.dptr, st);
   if (s == WK_OK) {
     cudaError_t ce = cudaMemcpyAsync(&bad, e->status.p, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
@@ -314,11 +320,11 @@ wk_status wk_engine_create(wk_layout *l, int dtype, const void *vals, const int3
   if (s == WK_OK && bad)
     s = set_error(WK_ERR_INVALID, "%d column indices lie outside [0, %u)", bad, ncols);
   if (s != WK_OK) {
+    e->layout = nullptr;
     delete e;
     return s;
   }
   l->refs.fetch_add(1);
-  e->layout = l;
   *out = e;
   return WK_OK;
 }
@@ -347,7 +353,7 @@ wk_status wk_engine_set_values(wk_engine *e, const void *vals, void *stream) {
   const size_t eb = dtype_size(e->dtype);
   DevView v;
   WK_TRY(v.from(vals, (size_t)e->layout->info.nz * eb, st));
-  WK_TRY(launch_process(e->layout, v.dptr, (int)eb, nullptr, e->vals.p, nullptr, false, st));
+  WK_TRY(load_values(e, v.dptr, st));
   if (v.tmp.p) WK_CUDA(cudaStreamSynchronize(st));
   return WK_OK;
 }
@@ -356,6 +362,13 @@ wk_status wk_engine_get_values(const wk_engine *e, void *dst, size_t cap) {
   if (!e || !dst) return set_error(WK_ERR_INVALID, "NULL argument");
   size_t n = e->layout->info.allocate_nz;
   if (cap < n) return set_error(WK_ERR_INVALID, "capacity %zu < %zu", cap, n);
+  if (n && e->dtype == WK_F16S) {  // the values the SpMV multiplies with, as FP32
+    DevBuf t;
+    WK_TRY(t.alloc(n * 4));
+    WK_TRY(launch_f16s_decode(e, t.as<float>(), nullptr));
+    WK_CUDA(cudaMemcpy(dst, t.p, n * 4, cudaMemcpyDefault));
+    return WK_OK;
+  }
   if (n) WK_CUDA(cudaMemcpy(dst, e->vals.p, n * dtype_size(e->dtype), cudaMemcpyDefault));
   return WK_OK;
 }

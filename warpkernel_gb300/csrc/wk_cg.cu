@@ -52,7 +52,8 @@ __global__ void __launch_bounds__(CG_BLOCK) k_spmv_dot(const V *__restrict__ pv,
                                                        const int4 *__restrict__ cdesc, const int4 *__restrict__ desc,
                                                        uint32_t W, const int32_t *__restrict__ row_map, uint32_t nzr,
                                                        uint32_t nrows, const X *__restrict__ p, X *__restrict__ q,
-                                                       const double *__restrict__ scal, double *__restrict__ partials) {
+                                                       const double *__restrict__ scal, double *__restrict__ partials,
+                                                       const float *__restrict__ wscale) {
   if (done(scal)) return;
   __shared__ double sh[32];
   const uint32_t lane = threadIdx.x & 31;
@@ -68,6 +69,7 @@ __global__ void __launch_bounds__(CG_BLOCK) k_spmv_dot(const V *__restrict__ pv,
     else
       s = lane_sum_fast<V, X, true>(pv, pc, d, p, lane, pol);
     s = row_tree(s, T);
+    if constexpr (Scaled<V>::value) s *= wscale[w];
     const uint32_t r = (uint32_t)d.w + lane / T;
     if (r < nzr && (lane & (T - 1)) == 0) {
       const int32_t row = row_map[r];
@@ -196,12 +198,15 @@ void cg_iteration(const wk_engine *e, const CgVectors<X> &v, double *scal, doubl
 #define WK_SPMV_DOT(V, COMP)                                                                                        \
   k_spmv_dot<V, X, COMP><<<g, CG_BLOCK, 0, st>>>(e->vals.as<V>(), e->cols.as<int32_t>(), e->c16.as<uint16_t>(),      \
                                                  e->c32.as<int32_t>(), e->cdesc.as<int4>(), l->d.warp_desc, W,        \
-                                                 l->d.row_map, l->info.nznrows, n, v.p, v.q, scal, partials)
+                                                 l->d.row_map, l->info.nznrows, n, v.p, v.q, scal, partials,       \
+                                                 e->scale.as<float>())
   if constexpr (sizeof(X) == 8) {
     if (e->compressed) WK_SPMV_DOT(double, true); else WK_SPMV_DOT(double, false);
   } else {
     if (e->dtype == WK_F32) {
       if (e->compressed) WK_SPMV_DOT(float, true); else WK_SPMV_DOT(float, false);
+    } else if (e->dtype == WK_F16S) {
+      if (e->compressed) WK_SPMV_DOT(__half, true); else WK_SPMV_DOT(__half, false);
     } else {
       if (e->compressed) WK_SPMV_DOT(__nv_bfloat16, true); else WK_SPMV_DOT(__nv_bfloat16, false);
     }
@@ -332,8 +337,8 @@ extern "C" wk_status wk_ir_cg(wk_engine *e64, wk_engine *lo, const double *b, do
   WK_TRY(require_interleaved(e64->layout, "wk_ir_cg"));
   WK_TRY(require_interleaved(lo->layout, "wk_ir_cg"));
   if (e64->dtype != WK_F64) return set_error(WK_ERR_INVALID, "wk_ir_cg: the residual engine must be WK_F64");
-  if (lo->dtype != WK_F32 && lo->dtype != WK_BF16)
-    return set_error(WK_ERR_INVALID, "wk_ir_cg: the inner engine must be WK_F32 or WK_BF16");
+  if (lo->dtype != WK_F32 && lo->dtype != WK_BF16 && lo->dtype != WK_F16S)
+    return set_error(WK_ERR_INVALID, "wk_ir_cg: the inner engine must be WK_F32, WK_BF16 or WK_F16S");
   WK_TRY(check_square(e64));
   if (lo->layout->info.nrows != e64->layout->info.nrows || lo->ncols != e64->ncols)
     return set_error(WK_ERR_INVALID, "wk_ir_cg: engines of different sizes");

@@ -39,7 +39,8 @@ unsigned grid_for(size_t n, int bs) {
 // order), WPK2 rows through the same lockstep tree as run.
 template <typename V>
 __global__ void k_assembly(const V *__restrict__ pv, const int4 *__restrict__ desc, uint32_t W,
-                           const int32_t *__restrict__ row_map, uint32_t nzr, typename core::Tr<V>::Acc *__restrict__ y) {
+                           const int32_t *__restrict__ row_map, uint32_t nzr, typename core::Tr<V>::Acc *__restrict__ y,
+                           const float *__restrict__ wscale) {
   typedef typename core::Tr<V>::Acc Acc;
   const uint32_t lane = threadIdx.x & 31;
   const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
@@ -56,6 +57,7 @@ __global__ void k_assembly(const V *__restrict__ pv, const int4 *__restrict__ de
     for (o += WS; o < end; o += WS) s += core::Tr<V>::acc(pv[o]);
   }
   s = core::row_tree(s, T);
+  if constexpr (core::Scaled<V>::value) s *= wscale[w];
   if (valid && (lane & (T - 1)) == 0) y[row_map[p]] = s;
 }
 
@@ -231,9 +233,10 @@ extern "C" wk_status wk_run_assembly(wk_engine *e, int nblocks, int blocksize, v
   if (l->info.nwarps) {
     const uint32_t W = l->info.nwarps, nzr = l->info.nznrows;
     switch (e->dtype) {
-      case WK_F64: k_assembly<double><<<grid, block, 0, st>>>(e->vals.as<double>(), l->d.warp_desc, W, l->d.row_map, nzr, (double *)dy); break;
-      case WK_F32: k_assembly<float><<<grid, block, 0, st>>>(e->vals.as<float>(), l->d.warp_desc, W, l->d.row_map, nzr, (float *)dy); break;
-      default: k_assembly<__nv_bfloat16><<<grid, block, 0, st>>>(e->vals.as<__nv_bfloat16>(), l->d.warp_desc, W, l->d.row_map, nzr, (float *)dy); break;
+      case WK_F64: k_assembly<double><<<grid, block, 0, st>>>(e->vals.as<double>(), l->d.warp_desc, W, l->d.row_map, nzr, (double *)dy, nullptr); break;
+      case WK_F32: k_assembly<float><<<grid, block, 0, st>>>(e->vals.as<float>(), l->d.warp_desc, W, l->d.row_map, nzr, (float *)dy, nullptr); break;
+      case WK_F16S: k_assembly<__half><<<grid, block, 0, st>>>(e->vals.as<__half>(), l->d.warp_desc, W, l->d.row_map, nzr, (float *)dy, e->scale.as<float>()); break;
+      default: k_assembly<__nv_bfloat16><<<grid, block, 0, st>>>(e->vals.as<__nv_bfloat16>(), l->d.warp_desc, W, l->d.row_map, nzr, (float *)dy, nullptr); break;
     }
     WK_CHECK_LAUNCH();
   }

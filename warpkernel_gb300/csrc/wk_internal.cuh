@@ -91,7 +91,10 @@ struct DevView {
 // Copies `bytes` from device `src` to caller memory `dst` (host or device).
 wk_status copy_out(void *dst, const void *src, size_t bytes, cudaStream_t stream);
 
+// Bytes per element of the values a caller passes and of x (WK_F16S: FP32).
 size_t dtype_size(int dtype);
+// Bytes per stored padded value (WK_F16S: 2).
+size_t stored_size(int dtype);
 
 // ---- handles ---------------------------------------------------------------------
 struct LayoutDev {
@@ -133,6 +136,7 @@ struct wk_engine {
   // compact 32-bit indices of the warps whose span needs them, per-warp descriptor
   bool compressed = false;
   wk::DevBuf c16, c32, cdesc;
+  wk::DevBuf scale;  // WK_F16S: float power-of-two scale per layout warp
 };
 
 namespace wk {
@@ -174,6 +178,11 @@ wk_status require_interleaved(const wk_layout *l, const char *op);
 // CSR-ordered values (elem bytes 8/4/2) and column indices.
 wk_status make_engine(wk_layout *l, int dtype, const void *d_vals, const int32_t *d_cols, uint32_t ncols,
                       cudaStream_t stream, wk_engine **out);
+// Places CSR-ordered device values (the engine's input type) into the padded
+// value array; WK_F16S values are scaled per warp and rounded to FP16.
+wk_status load_values(wk_engine *e, const void *d_vals, cudaStream_t stream);
+// WK_F16S: decodes the padded values to FP32 (allocate_nz floats, device).
+wk_status launch_f16s_decode(const wk_engine *e, float *out, cudaStream_t stream);
 // Builds / refreshes the engine's 16-bit column storage from its int32 columns.
 wk_status build_compressed_cols(wk_engine *e, cudaStream_t stream, uint32_t *wide_warps);
 

@@ -29,7 +29,8 @@ template <typename V, typename X, bool MAPPED, bool L1>
 __global__ void __launch_bounds__(1024) k_spmv_exact(const V *__restrict__ pv, const int32_t *__restrict__ pc,
                                                      const int4 *__restrict__ desc, uint32_t W,
                                                      const int32_t *__restrict__ row_map, uint32_t nzr,
-                                                     const X *__restrict__ x, typename Tr<V>::Acc *__restrict__ y) {
+                                                     const X *__restrict__ x, typename Tr<V>::Acc *__restrict__ y,
+                                                     const float *__restrict__ wscale) {
   const uint32_t lane = threadIdx.x & 31;
   const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
   if (w >= W) return;
@@ -39,6 +40,7 @@ __global__ void __launch_bounds__(1024) k_spmv_exact(const V *__restrict__ pv, c
   const bool valid = p < nzr;
   typename Tr<V>::Acc s = lane_sum_exact<V, X, L1>(pv, pc, d, x, lane, valid);
   s = row_tree(s, T);
+  if constexpr (Scaled<V>::value) s *= wscale[w];
   if (valid && (lane & (T - 1)) == 0) store_row<typename Tr<V>::Acc, MAPPED>(y, row_map, p, s);
 }
 
@@ -46,7 +48,8 @@ template <typename V, typename X, bool MAPPED, bool L1>
 __global__ void __launch_bounds__(1024) k_spmv_fast(const V *__restrict__ pv, const int32_t *__restrict__ pc,
                                                     const int4 *__restrict__ desc, uint32_t W,
                                                     const int32_t *__restrict__ row_map, uint32_t nzr,
-                                                    const X *__restrict__ x, typename Tr<V>::Acc *__restrict__ y) {
+                                                    const X *__restrict__ x, typename Tr<V>::Acc *__restrict__ y,
+                                                    const float *__restrict__ wscale) {
   const uint32_t lane = threadIdx.x & 31;
   const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
   if (w >= W) return;
@@ -55,6 +58,7 @@ __global__ void __launch_bounds__(1024) k_spmv_fast(const V *__restrict__ pv, co
   typename Tr<V>::Acc s = lane_sum_fast<V, X, L1>(pv, pc, d, x, lane, policy_evict_first());
   const uint32_t p = (uint32_t)d.w + lane / T;
   s = row_tree(s, T);
+  if constexpr (Scaled<V>::value) s *= wscale[w];
   if (p < nzr && (lane & (T - 1)) == 0) store_row<typename Tr<V>::Acc, MAPPED>(y, row_map, p, s);
 }
 
@@ -66,7 +70,8 @@ template <typename V, typename X, bool MAPPED, bool L1>
 __global__ void __launch_bounds__(1024) k_spmv_nocoal(const V *__restrict__ pv, const int32_t *__restrict__ pc,
                                                       const int4 *__restrict__ desc, uint32_t W,
                                                       const int32_t *__restrict__ row_map, uint32_t nzr,
-                                                      const X *__restrict__ x, typename Tr<V>::Acc *__restrict__ y) {
+                                                      const X *__restrict__ x, typename Tr<V>::Acc *__restrict__ y,
+                                                      const float *__restrict__ wscale) {
   typedef typename Tr<V>::Acc Acc;
   const uint32_t lane = threadIdx.x & 31;
   const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
@@ -79,6 +84,7 @@ __global__ void __launch_bounds__(1024) k_spmv_nocoal(const V *__restrict__ pv, 
   Acc s = Tr<V>::acc(pv[o]) * (Acc)Tr<X>::acc(gather<L1>(x, pc[o]));
   for (uint32_t i = 1; i < A; i++)
     s = fma_acc(Tr<V>::acc(pv[o + i]), (Acc)Tr<X>::acc(gather<L1>(x, pc[o + i])), s);
+  if constexpr (Scaled<V>::value) s *= wscale[w];
   store_row<Acc, MAPPED>(y, row_map, p, s);
 }
 
@@ -88,7 +94,8 @@ __global__ void __launch_bounds__(1024) k_spmv_fast_c(const V *__restrict__ pv, 
                                                       const int32_t *__restrict__ c32, const int4 *__restrict__ cdesc,
                                                       const int4 *__restrict__ desc, uint32_t W,
                                                       const int32_t *__restrict__ row_map, uint32_t nzr,
-                                                      const X *__restrict__ x, typename Tr<V>::Acc *__restrict__ y) {
+                                                      const X *__restrict__ x, typename Tr<V>::Acc *__restrict__ y,
+                                                      const float *__restrict__ wscale) {
   const uint32_t lane = threadIdx.x & 31;
   const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
   if (w >= W) return;
@@ -98,6 +105,7 @@ __global__ void __launch_bounds__(1024) k_spmv_fast_c(const V *__restrict__ pv, 
   typename Tr<V>::Acc s = lane_sum_compressed<V, X, L1>(pv, c16, c32, d, cd, x, lane, policy_evict_first());
   const uint32_t p = (uint32_t)d.w + lane / T;
   s = row_tree(s, T);
+  if constexpr (Scaled<V>::value) s *= wscale[w];
   if (p < nzr && (lane & (T - 1)) == 0) store_row<typename Tr<V>::Acc, MAPPED>(y, row_map, p, s);
 }
 
@@ -113,7 +121,8 @@ wk_status dispatch(const RunArgs &a, unsigned grid, unsigned block) {
   const int4 *desc = l->d.warp_desc;
   const int32_t *rm = l->d.row_map;
   const uint32_t W = l->info.nwarps, nzr = l->info.nznrows;
-#define WK_LAUNCH(K, M, C) K<V, X, M, C><<<grid, block, 0, a.stream>>>(pv, pc, desc, W, rm, nzr, x, y)
+  const float *ws = e->scale.as<float>();
+#define WK_LAUNCH(K, M, C) K<V, X, M, C><<<grid, block, 0, a.stream>>>(pv, pc, desc, W, rm, nzr, x, y, ws)
   const bool c = a.cache != 0;
   if (l->info.variant & WK_ABL_NOCOALESCE) {  // one order only: the reference's
     if (a.mapped) {
@@ -128,7 +137,7 @@ wk_status dispatch(const RunArgs &a, unsigned grid, unsigned block) {
     const uint16_t *c16 = e->c16.as<uint16_t>();
     const int32_t *c32 = e->c32.as<int32_t>();
     const int4 *cd = e->cdesc.as<int4>();
-#define WK_LAUNCH_C(M, C) k_spmv_fast_c<V, X, M, C><<<grid, block, 0, a.stream>>>(pv, c16, c32, cd, desc, W, rm, nzr, x, y)
+#define WK_LAUNCH_C(M, C) k_spmv_fast_c<V, X, M, C><<<grid, block, 0, a.stream>>>(pv, c16, c32, cd, desc, W, rm, nzr, x, y, ws)
     if (a.mapped) {
       if (c) WK_LAUNCH_C(true, true); else WK_LAUNCH_C(true, false);
     } else {
@@ -187,6 +196,7 @@ wk_status launch_spmv(const RunArgs &a) {
     case WK_F64: return dispatch<double, double>(a, grid, block);
     case WK_F32: return dispatch<float, float>(a, grid, block);
     case WK_BF16: return dispatch<__nv_bfloat16, __nv_bfloat16>(a, grid, block);
+    case WK_F16S: return dispatch<__half, float>(a, grid, block);
   }
   return set_error(WK_ERR_INVALID, "unknown dtype %d", a.e->dtype);
 }

@@ -8,7 +8,10 @@
 // summed by a tree (T_w = 1 for WPK1).
 #pragma once
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <stdint.h>
+
+#include <type_traits>
 
 namespace wk {
 namespace core {
@@ -74,6 +77,13 @@ __device__ __forceinline__ __nv_bfloat16 ld_stream1(const __nv_bfloat16 *p, uint
   return __ushort_as_bfloat16(v);
 }
 
+template <>
+__device__ __forceinline__ __half ld_stream1(const __half *p, uint64_t pol) {
+  unsigned short v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(v) : "l"(p), "l"(pol));
+  return __ushort_as_half(v);
+}
+
 // ---- type traits: value/vector element -> accumulator ------------------------------
 template <typename V>
 struct Tr;
@@ -91,6 +101,17 @@ template <>
 struct Tr<__nv_bfloat16> {
   typedef float Acc;
   static __device__ __forceinline__ float acc(__nv_bfloat16 v) { return __bfloat162float(v); }
+};
+// WK_F16S values: FP16 relative to the layout warp's power-of-two scale; the
+// kernels sum h * x in FP32 and multiply the row total by the scale (exact).
+template <>
+struct Tr<__half> {
+  typedef float Acc;
+  static __device__ __forceinline__ float acc(__half v) { return __half2float(v); }
+};
+template <typename V>
+struct Scaled {
+  static constexpr bool value = std::is_same<V, __half>::value;
 };
 
 // ---- gathers (x): L1-allocating (`cache`, the texture path of the reference) or L2 only
@@ -162,6 +183,10 @@ __device__ __forceinline__ float word_val<float>(const uint32_t *w, int k) {
 template <>
 __device__ __forceinline__ __nv_bfloat16 word_val<__nv_bfloat16>(const uint32_t *w, int k) {
   return __ushort_as_bfloat16((unsigned short)((k & 1) ? (w[k >> 1] >> 16) : (w[k >> 1] & 0xffffu)));
+}
+template <>
+__device__ __forceinline__ __half word_val<__half>(const uint32_t *w, int k) {
+  return __ushort_as_half((unsigned short)((k & 1) ? (w[k >> 1] >> 16) : (w[k >> 1] & 0xffffu)));
 }
 template <typename C>
 __device__ __forceinline__ int word_col(const uint32_t *w, int k, int base);

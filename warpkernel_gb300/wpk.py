@@ -18,14 +18,14 @@ import math
 import numpy as np
 
 from . import _lib
-from ._lib import (WK_BF16, WK_F32, WK_F64, WK_ORDER_EXACT, WK_ORDER_FAST, WK_WPK1, WK_WPK2,
+from ._lib import (WK_BF16, WK_F16S, WK_F32, WK_F64, WK_ORDER_EXACT, WK_ORDER_FAST, WK_WPK1, WK_WPK2,
                    LayoutInfo, check, load)
 
 __all__ = ["structure", "structure2", "engine", "profiler", "stats", "DTYPES",
            "WK_ORDER_FAST", "WK_ORDER_EXACT", "csr_matrix", "read_matrix_market_file"]
 
 DTYPES = {"f64": WK_F64, "float64": WK_F64, "f32": WK_F32, "float32": WK_F32,
-          "bf16": WK_BF16, "bfloat16": WK_BF16}
+          "bf16": WK_BF16, "bfloat16": WK_BF16, "f16s": WK_F16S}
 _NP_FIELD_DT = {"row_map": np.int32, "row_map_inv": np.int32, "reorder_rows": np.uint32,
                 "warp_offsets": np.int32, "max_nz_rows": np.uint32,
                 "threads_per_row": np.uint32, "row_offset_warp": np.uint32}
@@ -280,7 +280,8 @@ class engine:
         self.ncols = k.nrows if ncols is None else int(ncols)
         if A is None:
             return  # engine(structure&) of the reference: no arrays yet
-        A = _host_or_dev(A, {WK_F64: np.float64, WK_F32: np.float32}.get(self.dtype, np.uint16))
+        A = _host_or_dev(A, {WK_F64: np.float64, WK_F32: np.float32, WK_F16S: np.float32}.get(self.dtype,
+                                                                                            np.uint16))
         colinds = _host_or_dev(colinds, np.int32)
         ncols = k.nrows if ncols is None else int(ncols)
         h = C.c_void_p()
@@ -317,7 +318,7 @@ class engine:
 
     @property
     def device_values(self):
-        dt = {WK_F64: np.float64, WK_F32: np.float32, WK_BF16: np.uint16}[self.dtype]
+        dt = {WK_F64: np.float64, WK_F32: np.float32, WK_BF16: np.uint16, WK_F16S: np.float32}[self.dtype]
         a = np.zeros(self.kernel.allocate_nz, dt)
         check(load().wk_engine_get_values(self.handle, a.ctypes.data, a.size))
         return a
@@ -332,8 +333,8 @@ class engine:
     def set_values(self, A, stream=None):
         check(load().wk_engine_set_values(self.handle, _ptr(A), _stream_ptr(stream)))
 
-    _XDT = {WK_F64: "torch.float64", WK_F32: "torch.float32", WK_BF16: "torch.bfloat16"}
-    _YDT = {WK_F64: "torch.float64", WK_F32: "torch.float32", WK_BF16: "torch.float32"}
+    _XDT = {WK_F64: "torch.float64", WK_F32: "torch.float32", WK_BF16: "torch.bfloat16", WK_F16S: "torch.float32"}
+    _YDT = {WK_F64: "torch.float64", WK_F32: "torch.float32", WK_BF16: "torch.float32", WK_F16S: "torch.float32"}
 
     def _check_vectors(self, dx, dy, mapped):
         """Sizes and element types of tensor arguments (raw pointers cannot be
