@@ -18,11 +18,20 @@ namespace {
 
 using namespace core;
 
-constexpr int CG_BLOCK = 128;              // 4 warps per block in the SpMV-dot kernel
-constexpr unsigned CG_GRID = 152 * 12;     // blocks of the SpMV-dot kernel (grid-stride over layout warps)
+constexpr int CG_BLOCK = 128;              // 4 warps per block in the SpMV-dot kernel, one per layout warp
 constexpr int VEC_BLOCK = 256;
 constexpr unsigned VEC_GRID = 152 * 8;     // blocks of the vector kernels
-constexpr unsigned MAX_PARTIALS = CG_GRID > VEC_GRID ? CG_GRID : VEC_GRID;
+
+// Blocks of the SpMV-dot kernel (one warp per layout warp, like wk_run: a
+// grid-stride loop over layout warps measured 37 % slower at hex 96^3).
+unsigned spmv_dot_grid(const wk_layout *l) {
+  const size_t g = ((size_t)l->info.nwarps + CG_BLOCK / WS - 1) / (CG_BLOCK / WS);
+  return (unsigned)std::max<size_t>(1, g);
+}
+// Partial sums a CG run needs room for.
+size_t cg_partials(const wk_layout *l, unsigned residual_blocks) {
+  return std::max<size_t>({residual_blocks, VEC_GRID, spmv_dot_grid(l)});
+}
 
 // slots of `scal`
 enum { S_RHO0, S_RHO1, S_PQ, S_BB, S_RR64, S_TOL2, S_DONE, S_ITERS, S_MAXIT, S_COUNT };
@@ -57,10 +66,10 @@ __global__ void __launch_bounds__(CG_BLOCK) k_spmv_dot(const V *__restrict__ pv,
   if (done(scal)) return;
   __shared__ double sh[32];
   const uint32_t lane = threadIdx.x & 31;
-  const size_t nw = (size_t)gridDim.x * blockDim.x / WS;
   double part = 0.0;
   const uint64_t pol = policy_evict_first();
-  for (size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS; w < W; w += nw) {
+  const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
+  if (w < W) {
     const int4 d = desc[w];
     const uint32_t T = (uint32_t)d.z;
     typename Tr<V>::Acc s;
@@ -193,7 +202,7 @@ void cg_iteration(const wk_engine *e, const CgVectors<X> &v, double *scal, doubl
                   cudaStream_t st) {
   const wk_layout *l = e->layout;
   const uint32_t W = l->info.nwarps, n = l->info.nrows;
-  const unsigned g = std::max(1u, std::min(CG_GRID, (unsigned)((W + CG_BLOCK / WS - 1) / (CG_BLOCK / WS))));
+  const unsigned g = spmv_dot_grid(l);
   const int i_rho = parity ? S_RHO1 : S_RHO0, i_next = parity ? S_RHO0 : S_RHO1;
 #define WK_SPMV_DOT(V, COMP)                                                                                        \
   k_spmv_dot<V, X, COMP><<<g, CG_BLOCK, 0, st>>>(e->vals.as<V>(), e->cols.as<int32_t>(), e->c16.as<uint16_t>(),      \
@@ -296,7 +305,7 @@ extern "C" wk_status wk_cg(wk_engine *e, const double *b, double *x, wk_cg_param
   WK_TRY(pb.alloc((size_t)n * 8));
   WK_TRY(qb.alloc((size_t)n * 8));
   WK_TRY(sb.alloc(S_COUNT * 8));
-  WK_TRY(part.alloc((size_t)std::max(rg, MAX_PARTIALS) * 8));
+  WK_TRY(part.alloc(cg_partials(e->layout, rg) * 8));
   double *scal = sb.as<double>(), *pp = part.as<double>();
   CgVectors<double> v{x, rb.as<double>(), pb.as<double>(), qb.as<double>()};
   IterGraph gr;
@@ -355,7 +364,7 @@ extern "C" wk_status wk_ir_cg(wk_engine *e64, wk_engine *lo, const double *b, do
   WK_TRY(pb.alloc((size_t)n * 4));
   WK_TRY(qb.alloc((size_t)n * 4));
   WK_TRY(sb.alloc(S_COUNT * 8));
-  WK_TRY(part.alloc((size_t)std::max(rg, MAX_PARTIALS) * 8));
+  WK_TRY(part.alloc(std::max(cg_partials(lo->layout, rg), cg_partials(e64->layout, rg)) * 8));
   double *r64 = r64b.as<double>(), *scal = sb.as<double>(), *pp = part.as<double>();
   CgVectors<float> v{db.as<float>(), r32b.as<float>(), pb.as<float>(), qb.as<float>()};
   IterGraph gr;
