@@ -289,8 +289,7 @@ wk_status wk_csr_free(wk_csr *c);
  * DEVICE memory.  x (ncols), b, r (nrows) and norm2 are device pointers.  The
  * norm is reduced in a fixed order (bit-reproducible).  Uses an engine-owned
  * device buffer of per-block partial sums, allocated on the first call.
- * The residual of the iterative-refinement solve, which the spec asks
- * to keep in fp64. */
+ * It is the fp64 residual of the iterative-refinement solve (wk_ir_cg). */
 wk_status wk_residual(wk_engine *e, const double *x, const double *b, double *r, double *norm2,
                       void *stream);
 
@@ -312,7 +311,9 @@ wk_status wk_residual_static(wk_engine *e, const double *x, const double *b, dou
                              void *stream);
 
 /* Conjugate-gradient solves of A x = b for a symmetric positive definite A
- * (no reference counterpart; the north-star's refined solve).  Inputs: tol
+ * (no reference counterpart: an SpMV consumer that runs the WPK kernels in
+ * a solver loop, with an iterative-refinement form whose inner solve uses a
+ * low-precision engine).  Inputs: tol
  * (target ||b - A x|| / ||b||), max_iter (CG iterations, or outer refinement
  * steps for wk_ir_cg), max_inner / inner_tol (inner CG iterations and the
  * relative reduction each inner solve aims for), check_every (iterations
