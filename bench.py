@@ -16,7 +16,7 @@ L2, so no flush is needed between steps.
 restatement of the reference's WPK2 run, OpenMP across warps) on the host
 cores for the same workload; under torchrun only rank 0 runs it.
 
-Multi-GPU: the SpMV does not shard in this build (one GPU per matrix);
+Multi-GPU: one matrix's SpMV is not sharded (one GPU per matrix);
 --gpus N runs N independent replicas and reports the sum of their work over
 the slowest rank's time.
 """

@@ -2,8 +2,8 @@
  * wk_oracle.h -- CPU oracle for the WPK1/WPK2 SpMV path.
  *
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
- * algorithm (warpkernel.hpp of thejonwong/warpkernel) used as the checker for
- * the CUDA implementation.  Only tests/, __graft_entry__.smoke() and bench.py's
+ * algorithm (warpkernel.hpp of thejonwong/warpkernel) against which the CUDA
+ * implementation is tested.  Only tests/, __graft_entry__.smoke() and bench.py's
  * CPU-baseline / reference arms may load it.  The product library never links,
  * loads or calls anything in this directory.
  *

@@ -2,7 +2,7 @@
 the reference's own host scan compiled for the CPU (oracle/_ref/libwkref*.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
-bench.py's CPU arms as the checker.  The product package never imports it.
+bench.py's CPU arms, to check the CUDA path.  The product package never imports it.
 """
 from __future__ import annotations
 
