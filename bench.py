@@ -355,6 +355,29 @@ def suite_mixed_and_cg(reps):
     return res
 
 
+def suite_cg(iters, mesh=96):
+    """Profiling case: one fp64 CG of `iters` iterations (16-iteration graph
+    batches) on hex mesh^3 (3 dof, seed 2, WPK2 th=81), then one plain SpMV."""
+    import torch
+
+    import warpkernel_gb300 as wk
+    from warpkernel_gb300 import fe
+    rp, cols, vals = fe.fe_matrix(3, mesh, mesh, mesh, 3, 1, 2)
+    n, nnz = rp.numel() - 1, cols.numel()
+    k = wk.structure2().scan(nnz, n, None, rp, None, 81)
+    e64 = wk.engine(k, vals, cols)
+    xs = fe.uniform_vec(2, 1, n)
+    b = torch.zeros(n, dtype=torch.float64, device="cuda")
+    e64.run(0, 128, xs, b, order=1, timed=False)
+    x = torch.zeros_like(b)
+    res = wk.wpk.cg(e64, b, x, tol=1e-30, max_iter=iters, check_every=16)
+    y = torch.zeros_like(b)
+    spmv = e64.run(0, 128, xs, y)
+    return {"workload": f"hex{mesh}_3dof fp64 CG", "nrows": n, "nnz": nnz, "cg": res,
+            "ms_per_iteration": round(res["seconds"] * 1e3 / max(res["iters"], 1), 4),
+            "spmv_ms": round(spmv * 1e3, 4)}
+
+
 def suite_adjoint(reps):
     """hex 64^3 (3 dof, seed 4), fp32: forward SpMV vs forward + adjoint
     (dx = A^T dy and dvals) through the autograd binding's kernels."""
@@ -557,7 +580,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-suites", action="store_true",
                     help="skip the mixed-precision / CG / adjoint / batched measurements")
-    ap.add_argument("--only", choices=["mixed", "adjoint", "batched", "ablation"],
+    ap.add_argument("--only", choices=["mixed", "adjoint", "batched", "ablation", "cg"],
                     help="run one suite alone (profiling cases; --steps = timed repetitions, "
                          "batched: the first 128 matrices with a fixed threshold / tile)")
     args = ap.parse_args()
@@ -571,6 +594,8 @@ def main():
             res = suite_adjoint(reps)
         elif args.only == "ablation":
             res = suite_ablation(reps)
+        elif args.only == "cg":
+            res = suite_cg(reps, args.mesh)
         else:
             res = suite_batched(count=128, tune=False)
         print(json.dumps({"suite": args.only, **res}), flush=True)
