@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "wk_internal.cuh"
+#include "wk_spmv_core.cuh"
 
 namespace wk {
 namespace {
@@ -53,11 +54,43 @@ __device__ __forceinline__ void gather_tile(const T *__restrict__ xr, int jn, bo
   for (int j = 0; j < TR; j++) g[j] = j < jn ? __ldg(xr + j) : T(0);
 }
 
+// Value / column words of one unit of S steps (S slots of 32 B per lane).
+template <typename T>
+struct Unit {
+  static constexpr int S = 32 / (int)sizeof(T);  // float: 8 steps, double: 4
+  static constexpr int NWC = S;                   // column words per lane
+};
+
+template <typename T>
+__device__ __forceinline__ T staged_val(const uint32_t *sv, int q);
+template <>
+__device__ __forceinline__ float staged_val<float>(const uint32_t *sv, int q) {
+  return __uint_as_float(sv[q]);
+}
+template <>
+__device__ __forceinline__ double staged_val<double>(const uint32_t *sv, int q) {
+  return __hiloint2double((int)sv[2 * q + 1], (int)sv[2 * q]);
+}
+
+// The matrix stream of a layout warp is read a unit of S steps at a time
+// with one 32-byte load of values and one of columns per lane (the same
+// coalesced words lane_sum_vec reads), staged through shared memory in slot
+// order and read back as S consecutive steps of the lane's own layout lane,
+// so each lane keeps one accumulator per right-hand side.  The next unit's
+// loads are issued before the current unit's gathers.  Per lane the steps
+// are summed in order (fma from zero), which is the reference's order.
 template <typename T, int TR>
 __global__ void __launch_bounds__(BATCH_BLOCK) k_batch(const BatchMat<T> *__restrict__ mats,
                                                         const int4 *__restrict__ items, uint32_t nitems,
                                                         unsigned *__restrict__ counter) {
-  const uint32_t lane = threadIdx.x & 31;
+  constexpr int S = Unit<T>::S, NWC = Unit<T>::NWC;
+  constexpr int NSV = S * WS * (int)sizeof(T) / 4;  // staged value words per warp
+  __shared__ __align__(16) uint32_t s_val[BATCH_BLOCK / WS][NSV];
+  __shared__ __align__(16) int32_t s_col[BATCH_BLOCK / WS][S * WS];
+  const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x / WS;
+  uint32_t *sv = s_val[wib];
+  int32_t *sc = s_col[wib];
+  const uint64_t pol = core::policy_evict_first();
   for (;;) {
     unsigned it = 0;
     if (lane == 0) it = atomicAdd(counter, 1u);
@@ -72,15 +105,44 @@ __global__ void __launch_bounds__(BATCH_BLOCK) k_batch(const BatchMat<T> *__rest
       const uint32_t T_ = (uint32_t)d.z, A = (uint32_t)d.y;
       const uint32_t p = (uint32_t)d.w + lane / T_;
       const bool valid = p < M.nzr;
-      const size_t o = (size_t)(uint32_t)d.x + lane;
+      const size_t o = (size_t)(uint32_t)d.x;
+      const uint32_t units = A / S, rem = A % S;
       for (uint32_t j0 = 0; j0 < k; j0 += TR) {
         const int jn = (int)min((uint32_t)TR, k - j0);
         T acc[TR];
 #pragma unroll
         for (int j = 0; j < TR; j++) acc[j] = T(0);
-        size_t slot = o;
-#pragma unroll 2
-        for (uint32_t i = 0; i < A; i++, slot += WS) {
+        uint32_t wv[8], wc[NWC];
+        if (units) {
+          core::ld_words(M.vals + o + S * lane, wv, pol);
+          core::ld_words(M.cols + o + S * lane, wc, pol);
+        }
+        for (uint32_t u = 0; u < units; u++) {
+          __syncwarp();
+#pragma unroll
+          for (int q = 0; q < 8; q += 4)
+            *reinterpret_cast<uint4 *>(sv + 8 * lane + q) = make_uint4(wv[q], wv[q + 1], wv[q + 2], wv[q + 3]);
+#pragma unroll
+          for (int q = 0; q < NWC; q += 4)
+            *reinterpret_cast<uint4 *>(sc + NWC * lane + q) = make_uint4(wc[q], wc[q + 1], wc[q + 2], wc[q + 3]);
+          __syncwarp();
+          if (u + 1 < units) {
+            const size_t nxt = o + (size_t)(u + 1) * S * WS + S * lane;
+            core::ld_words(M.vals + nxt, wv, pol);
+            core::ld_words(M.cols + nxt, wc, pol);
+          }
+#pragma unroll
+          for (int st = 0; st < S; st++) {
+            const int q = st * WS + (int)lane;
+            const T v = staged_val<T>(sv, q);
+            T g[TR];
+            gather_tile<T, TR>(M.X + (size_t)sc[q] * ld + j0, jn, vec4, g);
+#pragma unroll
+            for (int j = 0; j < TR; j++) acc[j] = fma(v, g[j], acc[j]);
+          }
+        }
+        size_t slot = o + (size_t)units * S * WS + lane;
+        for (uint32_t i = 0; i < rem; i++, slot += WS) {
           const T v = __ldcs(M.vals + slot);
           const int c = __ldcs(M.cols + slot);
           T g[TR];
@@ -90,7 +152,7 @@ __global__ void __launch_bounds__(BATCH_BLOCK) k_batch(const BatchMat<T> *__rest
         }
 #pragma unroll
         for (int j = 0; j < TR; j++)
-          for (uint32_t s = 1; s < T_; s <<= 1) acc[j] += __shfl_down_sync(0xffffffffu, acc[j], s);
+          for (uint32_t s2 = 1; s2 < T_; s2 <<= 1) acc[j] += __shfl_down_sync(0xffffffffu, acc[j], s2);
         if (valid && (lane & (T_ - 1)) == 0) {
           T *yr = M.Y + (size_t)M.row_map[p] * ld + j0;
 #pragma unroll
