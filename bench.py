@@ -419,7 +419,7 @@ def suite_batched(count=512, tune=True):
 
     from warpkernel_gb300 import batched
     specs = batched.fe_matrix_set(512, seed=3)[:count]
-    tune = batched.autotune(specs, sample=128, reps=3) if tune else {"threshold_frac": 0.5, "rhs_tile": 8}
+    tune = batched.autotune(specs, sample=128, reps=3) if tune else {"threshold_frac": 1.0, "rhs_tile": 16}
     b = batched.Batch.from_fe(specs, "f32", tune["threshold_frac"], tune["rhs_tile"])
     X, Y = batched.make_vectors(specs)
     b.set_vectors(X, Y)
