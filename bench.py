@@ -408,6 +408,13 @@ def suite_adjoint(reps):
         tb = _event_ms(lambda: (fwd(), adj()), reps)
         out[order] = {"fwd_ms": round(tf, 4), "adj_ms": round(ta, 4), "fwd_plus_adj_ms": round(tb, 4),
                       "ratio": round(tb / tf, 3), "fused_symmetric_path": mat.symmetric}
+        if order == "slots":  # the same pair with 16-bit columns on both sides
+            mat.eng.compress_cols()
+            tf = _event_ms(fwd, reps)
+            ta = _event_ms(adj, reps)
+            tb = _event_ms(lambda: (fwd(), adj()), reps)
+            out["slots+cols16"] = {"fwd_ms": round(tf, 4), "adj_ms": round(ta, 4), "fwd_plus_adj_ms": round(tb, 4),
+                                   "ratio": round(tb / tf, 3)}
     return out
 
 

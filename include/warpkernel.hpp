@@ -228,6 +228,55 @@ class structure {
                                      reorder_A_rows.data(), nullptr));
     for (size_t i = 0; i < out.size(); i++) colinds[i] = out[i];
   }
+  /* reorder (warpkernel.hpp:380-398): the padded, interleaved values and
+   * columns (padding 0), built on the GPU. */
+  template <typename IndexType, typename ValueType>
+  void reorder(ValueType *A, IndexType *colinds, device_array<ValueType> &device_values,
+               device_array<IndexType> &device_colinds) {
+    static_assert(sizeof(IndexType) == 4, "32-bit column indices expected");
+    device_values.resize(allocate_nz);
+    device_colinds.resize(allocate_nz);
+    check(wk_process(handle(), dtype_of<ValueType>::value, A, reinterpret_cast<const int32_t *>(colinds),
+                     device_values.data(), reinterpret_cast<int32_t *>(device_colinds.data()), nullptr));
+  }
+  /* process (warpkernel.hpp:533-548): reorder plus device copies of row_map,
+   * max_nz_rows and warp_offsets. */
+  template <typename IndexType, typename ValueType>
+  void process(ValueType *A, IndexType *colinds, device_array<ValueType> &device_values,
+               device_array<IndexType> &device_colinds, device_array<IndexType> &device_row_map,
+               device_array<uint> &device_max_nz_per_row, device_array<IndexType> &device_warp_offsets) {
+    reorder(A, colinds, device_values, device_colinds);
+    device_row_map = row_map;
+    device_max_nz_per_row = max_nz_rows;
+    device_warp_offsets = warp_offsets;
+  }
+  /* reorder_values_coalesced (warpkernel.hpp:470-491): padded values only. */
+  template <typename ValueType, typename Array>
+  void reorder_values_coalesced(Array &values, device_array<ValueType> &dvalues) {
+    dvalues.resize(allocate_nz);
+    check(wk_process(handle(), dtype_of<ValueType>::value, &values[0], nullptr, dvalues.data(), nullptr, nullptr));
+  }
+  /* reorder_values_coalesced_GPU / reorder_columns_coalesced_GPU
+   * (warpkernel.hpp:494-503, 459-468): the same scatter from device arrays;
+   * the layout's own reorder_rows is used (the argument is accepted for the
+   * reference's signature). */
+  template <typename ValueType>
+  void reorder_values_coalesced_GPU(device_array<ValueType> &values, device_array<ValueType> &dvalues,
+                                    device_array<uint> &reorder_rows_) {
+    (void)reorder_rows_;
+    dvalues.resize(allocate_nz);
+    check(wk_process(handle(), dtype_of<ValueType>::value, values.data(), nullptr, dvalues.data(), nullptr, nullptr));
+  }
+  template <typename IndexType>
+  void reorder_columns_coalesced_GPU(device_array<IndexType> &values, device_array<IndexType> &dvalues,
+                                     device_array<uint> &reorder_rows_) {
+    static_assert(sizeof(IndexType) == 4, "32-bit column indices expected");
+    (void)reorder_rows_;
+    dvalues.resize(allocate_nz);
+    check(wk_process(handle(), WK_F32, nullptr, reinterpret_cast<const int32_t *>(values.data()), nullptr,
+                     reinterpret_cast<int32_t *>(dvalues.data()), nullptr));
+  }
+
   /* reorder_values_coalesced_rowsort (warpkernel.hpp:505-515), [CPU] as in
    * the reference: dvalues[reorder_rows[i]] = values[reorder_A_rows[i]]. */
   template <class HostArray, typename T>
@@ -316,6 +365,19 @@ class structure2 : public structure {
   template <class CSR, typename IndexType>
   void scan(uint &nz_, uint &nrows_, CSR &A, IndexType threshold) {
     scan(nz_, nrows_, &A.values[0], &A.row_offsets[0], &A.column_indices[0], threshold);
+  }
+
+  /* structure2::process (warpkernel.hpp:750-769): also threads_per_row and
+   * row_offset_warp on the device. */
+  template <typename IndexType, typename ValueType>
+  void process(ValueType *A, IndexType *colinds, device_array<ValueType> &device_values,
+               device_array<IndexType> &device_colinds, device_array<IndexType> &device_row_map,
+               device_array<uint> &device_max_nz_per_row, device_array<IndexType> &device_warp_offsets,
+               device_array<uint> &device_threads_per_row, device_array<uint> &device_row_offset_warp) {
+    structure::process(A, colinds, device_values, device_colinds, device_row_map, device_max_nz_per_row,
+                       device_warp_offsets);
+    device_threads_per_row = threads_per_row;
+    device_row_offset_warp = row_offset_warp;
   }
 
  protected:

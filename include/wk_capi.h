@@ -156,6 +156,17 @@ wk_status wk_reorder_columns(const wk_layout *l, const int32_t *cols, int32_t *o
 wk_status wk_reorder_columns_rowsort(const wk_layout *l, const int32_t *cols, int32_t *out_cols,
                                      int32_t *reorder_A_rows, void *stream);
 
+/* structure::reorder / process (warpkernel.hpp:380-398, 533-548, 750-769)
+ * into caller buffers: pvals gets allocate_nz values of `dtype` (WK_F64,
+ * WK_F32 or WK_BF16) and pcols allocate_nz column indices, padding slots 0;
+ * vals / cols are the nz CSR-ordered arrays.  Either output may be NULL
+ * (with its input), which also gives reorder_values_coalesced (470-491) and
+ * the reorder_*_coalesced_GPU scatters (459-468, 494-503).  Inputs and
+ * outputs host or device; columns are copied as given (not validated, not
+ * renumbered), as the reference copies them.  Synchronous. */
+wk_status wk_process(const wk_layout *l, int dtype, const void *vals, const int32_t *cols, void *pvals,
+                     int32_t *pcols, void *stream);
+
 /* structure::reorder_x(x, device_x) -- warpkernel.hpp:518-530:
  * x_out[row_map_inv[r]] = x[r].  dtype WK_F64 / WK_F32 / WK_BF16. */
 wk_status wk_reorder_x(const wk_layout *l, int dtype, const void *x, void *x_out, void *stream);

@@ -194,6 +194,25 @@ int main(int argc, char **argv) {
       std::printf("WPK2_rex_rowsort failed\n");
       failures++;
     }
+    // process / reorder (warpkernel.hpp:533-548, 750-769) into caller device arrays
+    {
+      device_array<ValueType> dv;
+      device_array<IndexType> dc, drm, dwo;
+      device_array<uint> dmx, dtpr, drow;
+      kernel1.process(&A_new_values[0], &reorder_cols[0], dv, dc, drm, dmx, dwo, dtpr, drow);
+      if (dv.to_host() != eng.device_values.to_host() || dc.to_host() != eng.device_colinds.to_host() ||
+          drm.to_host() != kernel1.row_map || dtpr.to_host() != kernel1.threads_per_row ||
+          drow.to_host() != kernel1.row_offset_warp || dwo.to_host() != kernel1.warp_offsets) {
+        std::printf("structure2::process differs from the engine's arrays\n");
+        failures++;
+      }
+      device_array<ValueType> dv2;
+      kernel1.reorder_values_coalesced(A_new_values, dv2);
+      if (dv2.to_host() != dv.to_host()) {
+        std::printf("reorder_values_coalesced differs\n");
+        failures++;
+      }
+    }
     device_array<ValueType> vslots;
     kernel1.reorder_values_coalesced_rowsort(A.values, vslots);
     if (vslots.to_host() != eng.device_values.to_host()) {

@@ -129,3 +129,32 @@ def test_engine_rejects_out_of_range_columns():
     bad[5] = 7
     with pytest.raises(wk().WKError, match="outside"):
         eng.device_colinds = bad
+
+
+def test_process_into_caller_buffers_matches_oracle():
+    """wk_process (structure::reorder / process, reorder_values_coalesced)
+    with host and device arrays, values and columns separately."""
+    import torch
+
+    import warpkernel_gb300 as wk
+    from conftest import random_csr
+    rng = np.random.default_rng(17)
+    rp, cols, vals = random_csr(rng, 1500, 45, p_empty=0.1)
+    for kind, th in ((1, 0), (2, 7)):
+        k = wk.structure() if kind == 1 else wk.structure2()
+        if kind == 1:
+            k.scan(len(cols), len(rp) - 1, None, rp)
+        else:
+            k.scan(len(cols), len(rp) - 1, None, rp, None, th)
+        with O.OracleLayout(rp, kind=kind, threshold=th) as L:
+            ov, oc = L.process(vals, cols)
+            pv, pc = k.process(vals, cols)
+            np.testing.assert_array_equal(pv, ov)
+            np.testing.assert_array_equal(pc, oc)
+            dv, dc = k.process(torch.from_numpy(vals).cuda(), torch.from_numpy(cols).cuda())
+            np.testing.assert_array_equal(dv.cpu().numpy(), ov)
+            np.testing.assert_array_equal(dc.cpu().numpy(), oc)
+            np.testing.assert_array_equal(k.reorder_values_coalesced(vals), ov)
+            assert k.process(None, cols)[0] is None
+            f32 = k.process(vals.astype(np.float32), None, dtype="f32")[0]
+            np.testing.assert_array_equal(f32, ov.astype(np.float32))

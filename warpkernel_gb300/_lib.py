@@ -94,6 +94,7 @@ SIGNATURES = {
     "wk_uniform_vec": (C.c_int, [u64, u64, vp, i64, vp]),
     "wk_convert": (C.c_int, [vp, C.c_int, vp, C.c_int, i64, vp]),
     "wk_reorder_columns_rowsort": (C.c_int, [vp, vp, vp, vp, vp]),
+    "wk_process": (C.c_int, [vp, C.c_int, vp, vp, vp, vp, vp]),
     "wk_run_assembly": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, _fp]),
     "wk_layout_save": (C.c_int, [vp, C.c_char_p]),
     "wk_layout_load": (C.c_int, [C.c_char_p, vp, _pvp]),

