@@ -216,6 +216,10 @@ enum {
   WK_ORDER_FAST = 0,  /* 256/128-bit loads; each lane's slots re-associated */
   WK_ORDER_EXACT = 1  /* the reference's order, bit-identical to the oracle  */
 };
+/* WK_ORDER_FAST on a layout of short warps (slot-weighted mean step count
+ * below 60 for 8-byte values, 16 for narrower ones) runs the exact-order
+ * kernel, which is the faster one there; its results then equal
+ * WK_ORDER_EXACT's and compressed columns are not used. */
 
 /* engine::run<cache>(nblocks, blocksize, dx, dy) -- warpkernel.hpp:811-860:
  * y[row_map[p]] = sum over row p.  dx: ncols device values, dy: nrows device

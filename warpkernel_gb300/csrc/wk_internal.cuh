@@ -120,6 +120,9 @@ struct wk_layout {
   wk_layout_info info{};
   wk::LayoutDev d;
   wk::DevBuf bufs[10];
+  // Slot-weighted mean of the warps' step counts (sum A_w^2 / sum A_w): the
+  // fast order runs the one-slot-per-step kernel when it is small.
+  double mean_steps = 0.0;
 };
 
 struct wk_engine {

@@ -321,6 +321,23 @@ __global__ void k_warp_tail(int32_t *warp_offsets, uint32_t *row_off, uint32_t W
   if (wpk2) row_off[W] = nrows;
 }
 
+__global__ void k_step_moments(const uint32_t *__restrict__ steps, uint32_t W, unsigned long long *__restrict__ m) {
+  unsigned long long a2 = 0, a1 = 0;
+  for (size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x; w < W; w += (size_t)gridDim.x * blockDim.x) {
+    const unsigned long long a = steps[w];
+    a2 += a * a;
+    a1 += a;
+  }
+  for (int o = 16; o; o >>= 1) {
+    a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+  }
+  if ((threadIdx.x & 31) == 0 && a1) {
+    atomicAdd(m, a2);
+    atomicAdd(m + 1, a1);
+  }
+}
+
 // reorder_rows[rowptr[row] + e] for every entry e of sorted row p.
 __global__ void k_reorder_rows(const WarpSplit *__restrict__ ws,
                                const unsigned long long *__restrict__ soff,
@@ -569,6 +586,15 @@ wk_status build_layout(wk_layout *l, const int32_t *d_rowptr, int kind, int32_t 
   }
   k_warp_tail<<<1, 1, 0, st>>>(d.warp_offsets, d.row_offset_warp, W, n, totals + 1, wpk2);
   WK_CHECK_LAUNCH();
+  if (W) {  // sum A_w^2 and sum A_w (exact integer sums, any order)
+    WK_CUDA(cudaMemsetAsync(tot.p, 0, 16, st));
+    k_step_moments<<<grid_for(W, 256), 256, 0, st>>>(d.max_nz_rows, W, totals);
+    WK_CHECK_LAUNCH();
+    unsigned long long hm[2];
+    WK_CUDA(cudaMemcpyAsync(hm, totals, sizeof hm, cudaMemcpyDeviceToHost, st));
+    WK_CUDA(cudaStreamSynchronize(st));
+    l->mean_steps = hm[1] ? (double)hm[0] / (double)hm[1] : 0.0;
+  }
 
   // 5. reorder_rows
   WK_TRY(l->bufs[2].alloc((size_t)nz * 4));

@@ -148,8 +148,18 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_exact(const V *__restric
   if (valid) {
     size_t o = (size_t)(uint32_t)d.x + lane;
     const size_t end = o + (size_t)WS * (uint32_t)d.y;
-    s = Tr<V>::acc(pv[o]) * (Acc)Tr<X>::acc(gather<L1>(x, pc[o]));
-    for (o += WS; o < end; o += WS) s = fma_acc(Tr<V>::acc(pv[o]), (Acc)Tr<X>::acc(gather<L1>(x, pc[o])), s);
+    if constexpr (sizeof(V) == 8) {
+      // 8-byte values: streaming loads with evict_first measured up to 25 %
+      // faster (hex 64^3, 2-D Q1 1024^2); for 4- and 2-byte values the plain
+      // loads were faster (up to 33 %), so those keep them.
+      const uint64_t pol = policy_evict_first();
+      s = Tr<V>::acc(ld_stream1(pv + o, pol)) * (Acc)Tr<X>::acc(gather<L1>(x, ld_stream1(pc + o, pol)));
+      for (o += WS; o < end; o += WS)
+        s = fma_acc(Tr<V>::acc(ld_stream1(pv + o, pol)), (Acc)Tr<X>::acc(gather<L1>(x, ld_stream1(pc + o, pol))), s);
+    } else {
+      s = Tr<V>::acc(pv[o]) * (Acc)Tr<X>::acc(gather<L1>(x, pc[o]));
+      for (o += WS; o < end; o += WS) s = fma_acc(Tr<V>::acc(pv[o]), (Acc)Tr<X>::acc(gather<L1>(x, pc[o])), s);
+    }
   }
   return s;
 }
