@@ -54,8 +54,10 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
   return t;  // valid in thread 0
 }
 
-// q = A p (rows without entries get 0) and block partials of p . q
-template <typename V, typename X, bool COMP>
+// q = A p (rows without entries get 0) and block partials of p . q.  MODE 0:
+// vector path, 1: vector path on 16-bit columns, 2: one slot per step (short
+// warps, as wk_run's fast order chooses).
+template <typename V, typename X, int MODE>
 __global__ void __launch_bounds__(CG_BLOCK) k_spmv_dot(const V *__restrict__ pv, const int32_t *__restrict__ pc,
                                                        const uint16_t *__restrict__ c16, const int32_t *__restrict__ c32,
                                                        const int4 *__restrict__ cdesc, const int4 *__restrict__ desc,
@@ -72,14 +74,16 @@ __global__ void __launch_bounds__(CG_BLOCK) k_spmv_dot(const V *__restrict__ pv,
   if (w < W) {
     const int4 d = desc[w];
     const uint32_t T = (uint32_t)d.z;
+    const uint32_t r = (uint32_t)d.w + lane / T;
     typename Tr<V>::Acc s;
-    if constexpr (COMP)
+    if constexpr (MODE == 1)
       s = lane_sum_compressed<V, X, true>(pv, c16, c32, d, cdesc[w], p, lane, pol);
+    else if constexpr (MODE == 2)
+      s = lane_sum_exact<V, X, true>(pv, pc, d, p, lane, r < nzr);
     else
       s = lane_sum_fast<V, X, true>(pv, pc, d, p, lane, pol);
     s = row_tree(s, T);
     if constexpr (Scaled<V>::value) s *= wscale[w];
-    const uint32_t r = (uint32_t)d.w + lane / T;
     if (r < nzr && (lane & (T - 1)) == 0) {
       const int32_t row = row_map[r];
       const X qv = (X)s;
@@ -204,23 +208,28 @@ void cg_iteration(const wk_engine *e, const CgVectors<X> &v, double *scal, doubl
   const uint32_t W = l->info.nwarps, n = l->info.nrows;
   const unsigned g = spmv_dot_grid(l);
   const int i_rho = parity ? S_RHO1 : S_RHO0, i_next = parity ? S_RHO0 : S_RHO1;
-#define WK_SPMV_DOT(V, COMP)                                                                                        \
-  k_spmv_dot<V, X, COMP><<<g, CG_BLOCK, 0, st>>>(e->vals.as<V>(), e->cols.as<int32_t>(), e->c16.as<uint16_t>(),      \
+  const int mode = short_layout(l, e->dtype) ? 2 : (e->compressed ? 1 : 0);
+#define WK_SPMV_DOT1(V, M)                                                                                          \
+  k_spmv_dot<V, X, M><<<g, CG_BLOCK, 0, st>>>(e->vals.as<V>(), e->cols.as<int32_t>(), e->c16.as<uint16_t>(),      \
                                                  e->c32.as<int32_t>(), e->cdesc.as<int4>(), l->d.warp_desc, W,        \
                                                  l->d.row_map, l->info.nznrows, n, v.p, v.q, scal, partials,       \
                                                  e->scale.as<float>())
+#define WK_SPMV_DOT(V)                                                                                              \
+  do {                                                                                                              \
+    if (mode == 2) WK_SPMV_DOT1(V, 2); else if (mode == 1) WK_SPMV_DOT1(V, 1); else WK_SPMV_DOT1(V, 0);             \
+  } while (0)
   if constexpr (sizeof(X) == 8) {
-    if (e->compressed) WK_SPMV_DOT(double, true); else WK_SPMV_DOT(double, false);
+    WK_SPMV_DOT(double);
   } else {
-    if (e->dtype == WK_F32) {
-      if (e->compressed) WK_SPMV_DOT(float, true); else WK_SPMV_DOT(float, false);
-    } else if (e->dtype == WK_F16S) {
-      if (e->compressed) WK_SPMV_DOT(__half, true); else WK_SPMV_DOT(__half, false);
-    } else {
-      if (e->compressed) WK_SPMV_DOT(__nv_bfloat16, true); else WK_SPMV_DOT(__nv_bfloat16, false);
-    }
+    if (e->dtype == WK_F32)
+      WK_SPMV_DOT(float);
+    else if (e->dtype == WK_F16S)
+      WK_SPMV_DOT(__half);
+    else
+      WK_SPMV_DOT(__nv_bfloat16);
   }
 #undef WK_SPMV_DOT
+#undef WK_SPMV_DOT1
   k_finish<false><<<1, 1024, 0, st>>>(partials, g, scal, S_PQ);
   k_update<X><<<VEC_GRID, VEC_BLOCK, 0, st>>>(v.x, v.r, v.p, v.q, n, scal, i_rho, partials);
   k_finish<true><<<1, 1024, 0, st>>>(partials, VEC_GRID, scal, i_next);

@@ -204,6 +204,12 @@ struct RunArgs {
   cudaStream_t stream;
 };
 wk_status launch_spmv(const RunArgs &a);
+// True if the layout's warps are short for `dtype` (slot-weighted mean step
+// count below 60 for 8-byte values, 16 for narrower ones): the one-slot-per-
+// step loop then beats the vector path.
+inline bool short_layout(const wk_layout *l, int dtype) {
+  return l->mean_steps < (dtype == WK_F64 ? 60.0 : 16.0);
+}
 // Grid / block of a one-warp-per-layout-warp launch (nblocks/blocksize <= 0: automatic).
 wk_status launch_shape(uint32_t W, int nblocks, int blocksize, unsigned *grid, unsigned *block);
 

@@ -136,8 +136,7 @@ wk_status dispatch(const RunArgs &a, unsigned grid, unsigned block) {
   // Fast order on layouts of short warps: the one-slot-per-step kernel beats
   // the vector path's cross-lane combine (break-even near 60 steps for 8-byte
   // values, 16 for narrower ones; hex 64^3 thresholds 2-81 and 2-D Q1 1024^2).
-  const double short_steps = sizeof(V) == 8 ? 60.0 : 16.0;
-  const bool use_exact = a.order == WK_ORDER_EXACT || l->mean_steps < short_steps;
+  const bool use_exact = a.order == WK_ORDER_EXACT || short_layout(l, e->dtype);
   if (e->compressed && !use_exact) {
     const uint16_t *c16 = e->c16.as<uint16_t>();
     const int32_t *c32 = e->c32.as<int32_t>();
