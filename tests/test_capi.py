@@ -87,3 +87,25 @@ def test_python_mirror_names_match_reference_surface():
     s.add(1.0, "b")
     s.add(5.0, "c")
     assert (s.Min(), s.Min_str(), s.Max(), s.Max_str()) == (1.0, "b", 5.0, "c")
+
+
+def test_cpp_drop_in_header_compiles_and_links(tmp_path):
+    """include/warpkernel.hpp and the driver written against it compile and
+    link on a machine without a GPU (running it is a GPU test)."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not gxx or not os.path.exists(nvcc):
+        pytest.skip("g++ or the CUDA toolkit is missing")
+    cuda = os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
+    libdir = os.path.join(ROOT, "warpkernel_gb300")
+    if not os.path.exists(os.path.join(libdir, "libwarpkernel_gb300.so")):
+        pytest.skip("library not built")
+    exe = str(tmp_path / "wpk_driver")
+    cmd = [gxx, "-O1", "-std=c++17", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+           "-I", os.path.join(cuda, "include"), os.path.join(ROOT, "tests", "cpp", "wpk_driver.cpp"), "-o", exe,
+           "-L", libdir, "-lwarpkernel_gb300", "-L", os.path.join(cuda, "lib64"), "-L", os.path.join(cuda, "lib"),
+           "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]

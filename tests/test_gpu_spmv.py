@@ -234,3 +234,33 @@ def test_compressed_columns_bit_identical_to_uncompressed():
                 assert t.equal(y0, y3)
         if n == 200_000:
             assert wide > 0  # random columns leave warps in 32-bit mode
+
+
+def test_concurrent_streams_give_the_sequential_results():
+    """Calls are stream-ordered and handles independent: two engines (and
+    one engine on two output vectors) launched on two streams without
+    synchronising in between give the results of sequential runs."""
+    t = torch()
+    rp1, c1, v1 = O.fe_matrix(3, 10, 9, 8, 3, value_mode=1, seed=11)
+    rp2, c2, v2 = O.fe_matrix(2, 150, 140, 0, 1, value_mode=0, seed=12)
+    e1 = make(2, rp1, c1, v1, th=81)[1]
+    e2 = make(1, rp2, c2, v2)[1]
+    n1, n2 = len(rp1) - 1, len(rp2) - 1
+    x1 = t.from_numpy(O.uniform_vec(1, 0, n1)).cuda()
+    x2 = t.from_numpy(O.uniform_vec(2, 0, n2)).cuda()
+    ref = []
+    for e, x, n in ((e1, x1, n1), (e2, x2, n2), (e1, x1, n1)):
+        y = t.zeros(n, dtype=t.float64, device="cuda")
+        e.run(0, 128, x, y, order=0, timed=False)
+        t.cuda.synchronize()
+        ref.append(y)
+    s1, s2 = t.cuda.Stream(), t.cuda.Stream()
+    ys = [t.full((n,), float("nan"), dtype=t.float64, device="cuda") for n in (n1, n2, n1)]
+    t.cuda.synchronize()
+    for rep in range(20):
+        e1.run(0, 128, x1, ys[0], order=0, stream=s1, timed=False)
+        e2.run(0, 128, x2, ys[1], order=0, stream=s2, timed=False)
+        e1.run(0, 128, x1, ys[2], order=0, stream=s2, timed=False)
+    t.cuda.synchronize()
+    for y, r in zip(ys, ref):
+        assert t.equal(y, r)
