@@ -408,7 +408,16 @@ def suite_adjoint(reps):
         tb = _event_ms(lambda: (fwd(), adj()), reps)
         out[order] = {"fwd_ms": round(tf, 4), "adj_ms": round(ta, 4), "fwd_plus_adj_ms": round(tb, 4),
                       "ratio": round(tb / tf, 3), "fused_symmetric_path": mat.symmetric}
-        if order == "slots":  # the same pair with 16-bit columns on both sides
+        if order == "slots":
+            # dx = A^T dy alone (no dvals): the adjoint a linear solve's gradient needs
+            def adj_dx():
+                mat.adjoint(x, dy, want_dx=True, want_dvals=False)
+
+            td = _event_ms(adj_dx, reps)
+            tbd = _event_ms(lambda: (fwd(), adj_dx()), reps)
+            out["dx_only"] = {"fwd_ms": round(tf, 4), "adj_ms": round(td, 4), "fwd_plus_adj_ms": round(tbd, 4),
+                              "ratio": round(tbd / tf, 3)}
+            # the same pair with 16-bit columns on both sides
             mat.eng.compress_cols()
             tf = _event_ms(fwd, reps)
             ta = _event_ms(adj, reps)
@@ -416,6 +425,30 @@ def suite_adjoint(reps):
             out["slots+cols16"] = {"fwd_ms": round(tf, 4), "adj_ms": round(ta, 4), "fwd_plus_adj_ms": round(tb, 4),
                                    "ratio": round(tb / tf, 3)}
     return out
+
+
+def suite_f16s(reps, mesh=96):
+    """hex mesh^3 (3 dof, seed 2, WPK2 threshold 81): the scaled-FP16
+    (WK_F16S) engine alone, FP32 x and y; GB/s counts 2 B value + 4 B column
+    per nonzero and 4 B x + 4 B y + 4 B row map per row."""
+    import numpy as np
+    import torch
+
+    import warpkernel_gb300 as wk
+    from oracle import wk_oracle as O
+    from warpkernel_gb300 import fe
+    rp, cols, vals = fe.fe_matrix(3, mesh, mesh, mesh, 3, 1, 2)
+    n, nnz = rp.numel() - 1, cols.numel()
+    x = fe.uniform_vec(2, 0, n)
+    k = wk.structure2().scan(nnz, n, None, rp, None, 81)
+    e = wk.engine(k, fe.convert(vals, torch.float32), cols, dtype="f16s")
+    xd = x.float()
+    yd = torch.zeros(n, dtype=torch.float32, device="cuda")
+    ms = _event_ms(lambda: e.run(0, 128, xd, yd, timed=False), reps)
+    y_ref = O.csr_spmv(rp.cpu().numpy(), cols.cpu().numpy(), vals.cpu().numpy(), x.cpu().numpy())
+    err = float(np.linalg.norm(yd.double().cpu().numpy() - y_ref) / np.linalg.norm(y_ref))
+    return {"workload": f"hex{mesh}_3dof seed 2 f16s", "nrows": n, "nnz": nnz, "ms": round(ms, 4),
+            "gbs": round((6 * nnz + 12 * n) / ms / 1e6, 1), "rel_err": err}
 
 
 def suite_batched(count=512, tune=True):
@@ -587,7 +620,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-suites", action="store_true",
                     help="skip the mixed-precision / CG / adjoint / batched measurements")
-    ap.add_argument("--only", choices=["mixed", "adjoint", "batched", "ablation", "cg"],
+    ap.add_argument("--only", choices=["mixed", "adjoint", "batched", "ablation", "cg", "f16s"],
                     help="run one suite alone (profiling cases; --steps = timed repetitions, "
                          "batched: the first 128 matrices with a fixed threshold / tile)")
     args = ap.parse_args()
@@ -603,6 +636,8 @@ def main():
             res = suite_ablation(reps)
         elif args.only == "cg":
             res = suite_cg(reps, args.mesh)
+        elif args.only == "f16s":
+            res = suite_f16s(reps, args.mesh)
         else:
             res = suite_batched(count=128, tune=False)
         print(json.dumps({"suite": args.only, **res}), flush=True)
