@@ -191,9 +191,11 @@ def test_fp32_and_value_updates():
 
 @pytest.mark.parametrize("value_order", ["csr", "slots"])
 def test_one_sided_adjoints_match_the_full_adjoint(value_order):
-    """dx alone (x needs a gradient, vals do not) and dvals alone give the
-    same bits as the run that computes both, on the fused symmetric path
-    and on the transposed-layout path."""
+    """dx alone (x needs a gradient, vals do not) and dvals alone against the
+    run that computes both, on the fused symmetric path and on the
+    transposed-layout path.  dvals are single products: the same bits.  dx
+    alone runs the transposed engine's SpMV, whose sums may be ordered
+    differently from the fused kernel's: equal to rounding (fp64)."""
     import torch
 
     from warpkernel_gb300.autograd import WPKMatrix
@@ -213,6 +215,7 @@ def test_one_sided_adjoints_match_the_full_adjoint(value_order):
         dx1, dv1 = m.adjoint(x, dy, want_dx=True, want_dvals=False)
         dx2, dv2 = m.adjoint(x, dy, want_dx=False, want_dvals=True)
         assert dv1 is None and dx2 is None
-        assert torch.equal(dx1, dx) and torch.equal(dv2, dv)
+        assert torch.equal(dv2, dv)
+        assert rel(dx1.cpu().numpy(), dx.cpu().numpy()) < 1e-14
         y_ref = O.csr_spmv_t(rp, cols, vals, dy.cpu().numpy(), n)
         assert rel(dx1.cpu().numpy(), y_ref) < 1e-12
