@@ -17,8 +17,9 @@
  *  - run / run_x compute every row whatever the grid size (the reference's
  *    2-D grid for nblocks > 65535 skipped rows, warpkernel.hpp:818-826) and
  *    reject grids that do not cover all warps;
- *  - the `cache` template flag selects L1-allocating x gathers (true) or
- *    L2-only gathers (false); there are no texture references.
+ *  - the `cache` template flag selects read-only non-coherent x gathers
+ *    (true, the texture path) or plain L1-caching loads (false, the
+ *    reference's x[i]); there are no texture references.
  *
  * Needs the CUDA runtime headers (cuda_runtime.h) and links against
  * libwarpkernel_gb300.so and the CUDA runtime.

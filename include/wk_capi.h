@@ -217,7 +217,7 @@ enum {
   WK_ORDER_EXACT = 1  /* the reference's order, bit-identical to the oracle  */
 };
 /* WK_ORDER_FAST on a layout of short warps (slot-weighted mean step count
- * below 60 for 8-byte values, 16 for narrower ones) runs the exact-order
+ * below 48 for fp64, 20 for fp32 and bf16, 16 for scaled FP16) runs the exact-order
  * kernel, which is the faster one there; its results then equal
  * WK_ORDER_EXACT's and compressed columns are not used. */
 
@@ -227,7 +227,8 @@ enum {
  * engines).  blocksize: threads per block (a multiple of 32, <= 1024);
  * nblocks must cover nwarps / (blocksize/32) blocks; nblocks <= 0 or
  * blocksize <= 0 selects the launch shape automatically.  cache != 0 gathers
- * x through L1 (the texture-cache path of the reference), 0 through L2 only.
+ * x with read-only non-coherent loads (the texture-cache path of the
+ * reference), 0 with plain L1-caching loads (the reference's x[i]).
  * If `seconds` is non-NULL the call synchronises and stores the kernel time
  * measured with CUDA events (the reference returns elapsed seconds);
  * otherwise it returns right after the launch.  Rows without entries are not

@@ -264,3 +264,37 @@ def test_concurrent_streams_give_the_sequential_results():
     t.cuda.synchronize()
     for y, r in zip(ys, ref):
         assert t.equal(y, r)
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32", "bf16", "f16s"])
+def test_fast_order_on_short_warps_is_the_exact_order(dtype):
+    """Layouts whose slot-weighted mean step count is below the type's
+    crossover (2-D Q1, 9 entries per row: 9 steps) run the one-slot-per-step
+    kernel in fast order: same bits as WK_ORDER_EXACT, for both x paths and
+    with 16-bit columns.  A long-warp layout (hex, 3 dof: 81 steps) takes the
+    vector path and stays within the fast-order tolerance."""
+    t = torch()
+    tdt = {"f64": t.float64, "f32": t.float32, "bf16": t.bfloat16, "f16s": t.float32}[dtype]
+    ydt = t.float64 if dtype == "f64" else t.float32
+    for rp, cols, vals, short in ((*O.fe_matrix(2, 60, 60, 0, 1, value_mode=1, seed=2), True),
+                                  (*O.fe_matrix(3, 8, 8, 8, 3, value_mode=1, seed=2), False)):
+        n = len(rp) - 1
+        k = wk().structure()
+        k.scan(len(cols), n, None, rp)
+        eng = wk().engine(k, wk().fe.convert(t.from_numpy(vals).cuda(), tdt), t.from_numpy(cols).cuda(), dtype=dtype)
+        x = wk().fe.convert(t.from_numpy(O.uniform_vec(5, 0, n)).cuda(), tdt)
+        ys = {}
+        for comp in (False, True):
+            if comp:
+                eng.compress_cols()
+            for cache in (True, False):
+                for order in (0, 1):
+                    y = t.zeros(n, dtype=ydt, device="cuda")
+                    eng.run(0, 128, x, y, cache=cache, order=order)
+                    ys[(comp, cache, order)] = y
+        for key, y in ys.items():
+            assert t.equal(y, ys[(False, True, 1)]) or not short, (dtype, key)
+            if not short:
+                ref = ys[(False, True, 1)].double()
+                rel = float((y.double() - ref).norm() / ref.norm())
+                assert rel < (1e-12 if dtype == "f64" else 1e-5), (dtype, key, rel)

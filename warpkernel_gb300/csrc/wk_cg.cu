@@ -77,11 +77,11 @@ __global__ void __launch_bounds__(CG_BLOCK) k_spmv_dot(const V *__restrict__ pv,
     const uint32_t r = (uint32_t)d.w + lane / T;
     typename Tr<V>::Acc s;
     if constexpr (MODE == 1)
-      s = lane_sum_compressed<V, X, true>(pv, c16, c32, d, cdesc[w], p, lane, pol);
+      s = lane_sum_compressed<V, X, true, false>(pv, c16, c32, d, cdesc[w], p, lane, pol);
     else if constexpr (MODE == 2)
       s = lane_sum_exact<V, X, true>(pv, pc, d, p, lane, r < nzr);
     else
-      s = lane_sum_fast<V, X, true>(pv, pc, d, p, lane, pol);
+      s = lane_sum_fast<V, X, true, false>(pv, pc, d, p, lane, pol);
     s = row_tree(s, T);
     if constexpr (Scaled<V>::value) s *= wscale[w];
     if (r < nzr && (lane & (T - 1)) == 0) {

@@ -204,12 +204,21 @@ struct RunArgs {
   cudaStream_t stream;
 };
 wk_status launch_spmv(const RunArgs &a);
-// True if the layout's warps are short for `dtype` (slot-weighted mean step
-// count below 60 for 8-byte values, 16 for narrower ones): the one-slot-per-
-// step loop then beats the vector path.
-inline bool short_layout(const wk_layout *l, int dtype) {
-  return l->mean_steps < (dtype == WK_F64 ? 60.0 : 16.0);
+// True if the layout's warps are short for `dtype`: the one-slot-per-step
+// loop then beats the vector path.  Crossovers of the slot-weighted mean step
+// count measured on hex meshes (1-3 dof, WPK2 thresholds giving 6-81 steps):
+// fp64 between 41 and 54 steps, fp32 and bf16 near 25 with 32-bit columns and
+// near 17 with 16-bit ones, scaled FP16 near 10.  One value per type keeps
+// the 16-bit column form's sums bit-identical to the 32-bit form's.
+inline double short_steps(int dtype) {
+  switch (dtype) {
+    case WK_F64: return 48.0;
+    case WK_F32:
+    case WK_BF16: return 20.0;
+    default: return 16.0;
+  }
 }
+inline bool short_layout(const wk_layout *l, int dtype) { return l->mean_steps < short_steps(dtype); }
 // Grid / block of a one-warp-per-layout-warp launch (nblocks/blocksize <= 0: automatic).
 wk_status launch_shape(uint32_t W, int nblocks, int blocksize, unsigned *grid, unsigned *block);
 

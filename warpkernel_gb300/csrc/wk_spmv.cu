@@ -4,11 +4,13 @@
 //  * exact: one slot per lane per step in the reference's order (first
 //    product, then fma per step, then the tree) -- bit-identical to the oracle
 //    and to the reference kernels compiled with contraction;
-//  * fast: 4 slots per lane per iteration with 256/128-bit loads, rows
+//  * fast: several slots per lane per iteration (VecPlan: 4 for fp64, 8 for
+//    fp32 and scaled FP16, 16 for bf16) with 256/128-bit loads, rows
 //    re-associated.
 // The matrix stream is loaded with ld.global.nc.L1::no_allocate and an L2
-// evict_first policy so that x (gathered through L1 with cache != 0, or L2
-// only with cache == 0) stays resident in L2.  One warp per layout warp.
+// evict_first policy so that x (gathered with ld.global.nc with cache != 0,
+// ld.global.ca with cache == 0) stays resident in L2.  One warp per layout
+// warp.
 #include "wk_internal.cuh"
 #include "wk_spmv_core.cuh"
 
@@ -134,8 +136,7 @@ wk_status dispatch(const RunArgs &a, unsigned grid, unsigned block) {
     return WK_OK;
   }
   // Fast order on layouts of short warps: the one-slot-per-step kernel beats
-  // the vector path's cross-lane combine (break-even near 60 steps for 8-byte
-  // values, 16 for narrower ones; hex 64^3 thresholds 2-81 and 2-D Q1 1024^2).
+  // the vector path's cross-lane combine (short_steps gives the crossovers).
   const bool use_exact = a.order == WK_ORDER_EXACT || short_layout(l, e->dtype);
   if (e->compressed && !use_exact) {
     const uint16_t *c16 = e->c16.as<uint16_t>();

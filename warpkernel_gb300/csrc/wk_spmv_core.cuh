@@ -114,15 +114,21 @@ struct Scaled {
   static constexpr bool value = std::is_same<V, __half>::value;
 };
 
-// ---- gathers (x): L1-allocating (`cache`, the texture path of the reference) or L2 only
+// ---- gathers (x).  `cache` (the reference's texture fetch, fetch_cache<true>
+// in warpkernel.hpp:41-49) reads through the non-coherent read-only path
+// (ld.global.nc); without it the reference reads x[i] with a plain global
+// load, which on sm_103a caches in L1 (ld.global.ca).  (On the Kepler parts
+// the reference targeted a plain load bypassed L1; an L2-only gather here
+// measured 3.6x slower on split rows, whose lanes revisit the same x sectors
+// step after step.)
 template <bool L1>
-__device__ __forceinline__ double gather(const double *x, int i) { return L1 ? __ldg(x + i) : __ldcg(x + i); }
+__device__ __forceinline__ double gather(const double *x, int i) { return L1 ? __ldg(x + i) : __ldca(x + i); }
 template <bool L1>
-__device__ __forceinline__ float gather(const float *x, int i) { return L1 ? __ldg(x + i) : __ldcg(x + i); }
+__device__ __forceinline__ float gather(const float *x, int i) { return L1 ? __ldg(x + i) : __ldca(x + i); }
 template <bool L1>
 __device__ __forceinline__ __nv_bfloat16 gather(const __nv_bfloat16 *x, int i) {
   const unsigned short *u = reinterpret_cast<const unsigned short *>(x);
-  return __ushort_as_bfloat16(L1 ? __ldg(u + i) : __ldcg(u + i));
+  return __ushort_as_bfloat16(L1 ? __ldg(u + i) : __ldca(u + i));
 }
 
 __device__ __forceinline__ double fma_acc(double a, double b, double c) { return fma(a, b, c); }
@@ -148,10 +154,11 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_exact(const V *__restric
   if (valid) {
     size_t o = (size_t)(uint32_t)d.x + lane;
     const size_t end = o + (size_t)WS * (uint32_t)d.y;
-    if constexpr (sizeof(V) == 8) {
-      // 8-byte values: streaming loads with evict_first measured up to 25 %
-      // faster (hex 64^3, 2-D Q1 1024^2); for 4- and 2-byte values the plain
-      // loads were faster (up to 33 %), so those keep them.
+    if constexpr (sizeof(V) == 8 || Scaled<V>::value) {
+      // 8-byte values and scaled FP16 (FP32 x): streaming loads with
+      // evict_first measured up to 25 % faster (hex 64^3, 2-D Q1 1024^2);
+      // for fp32 and bf16 the plain loads were faster (up to 33 %), so those
+      // keep them.
       const uint64_t pol = policy_evict_first();
       s = Tr<V>::acc(ld_stream1(pv + o, pol)) * (Acc)Tr<X>::acc(gather<L1>(x, ld_stream1(pc + o, pol)));
       for (o += WS; o < end; o += WS)
@@ -179,6 +186,10 @@ __device__ __forceinline__ void ld_words(const void *p, uint32_t (&w)[8], uint64
   asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8], %9;"
                : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]), "=r"(w[6]), "=r"(w[7])
                : "l"(p), "l"(pol));
+}
+__device__ __forceinline__ void ld_words(const void *p, uint32_t (&w)[16], uint64_t pol) {
+  ld_words(p, *reinterpret_cast<uint32_t(*)[8]>(&w[0]), pol);
+  ld_words((const char *)p + 32, *reinterpret_cast<uint32_t(*)[8]>(&w[8]), pol);
 }
 template <typename V>
 __device__ __forceinline__ V word_val(const uint32_t *w, int k);
@@ -221,6 +232,27 @@ template <typename V>
 struct SlotsPerLane {
   static constexpr int value = sizeof(V) == 8 ? 4 : 8;
 };
+// Per (value, column) type: slots per lane and whether the next unit's
+// loads are issued before this unit's gathers (software pipelining), chosen
+// by measurement on hex 96^3 (3 dof) on four GB300s.  bf16 streams 16 slots
+// per lane (32 B of values, 256-bit loads): 3 % faster with 32-bit columns,
+// 1-11 % with 16-bit ones, and the same slot count for both column types
+// keeps their sums bit-identical.  fp32 with 32-bit columns is pipelined
+// (3 % faster on every box).  Pipelining the other forms was faster on some
+// boxes and slower on others, so they keep the plain loop.
+template <typename V, typename C>
+struct VecPlan {
+  static constexpr int slots = std::is_same<V, __nv_bfloat16>::value ? 16 : SlotsPerLane<V>::value;
+  static constexpr bool pipelined = sizeof(V) == 4 && sizeof(C) == 4;
+};
+// The CG's SpMV-dot (FP32 p for every narrow value type, plus the dot
+// product) keeps 8 slots and the plain loop: the plan above raised its
+// registers from 40-48 to 64 and slowed the FP32 / bf16 inner solves by 4 %.
+template <typename V, typename C>
+struct PlainPlan {
+  static constexpr int slots = SlotsPerLane<V>::value;
+  static constexpr bool pipelined = false;
+};
 
 // Fast order: with S slots per lane, a unit of S steps is 32*S consecutive
 // slots; lane j streams slots S*j .. S*j+S-1 (layout lanes S*(j%R) .. +S-1 at
@@ -231,12 +263,13 @@ struct SlotsPerLane {
 // cp0 points at the warp's first column entry (slot o_w of a slot-indexed
 // array, or the warp's start in a compact array); base is added to 16-bit
 // offsets.
-template <typename V, typename X, bool L1, typename C>
+template <typename V, typename X, bool L1, typename C, bool TUNED = true>
 __device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict__ pv, const C *__restrict__ cp0, int base,
                                                            int4 d, const X *__restrict__ x, uint32_t lane,
                                                            uint64_t pol) {
   typedef typename Tr<V>::Acc Acc;
-  constexpr int S = SlotsPerLane<V>::value;
+  typedef typename std::conditional<TUNED, VecPlan<V, C>, PlainPlan<V, C>>::type Plan;
+  constexpr int S = Plan::slots;
   constexpr int R = 32 / S;
   constexpr int NWV = S * (int)sizeof(V) / 4, NWC = S * (int)sizeof(C) / 4;
   const uint32_t A = (uint32_t)d.y;
@@ -247,6 +280,30 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict_
   for (int k = 0; k < S; k++) a[k] = Acc(0);
   const V *vp = pv + o + S * lane;
   const C *cp = cp0 + S * lane;
+  if constexpr (Plan::pipelined) {
+    uint32_t wv[NWV], wc[NWC];
+    if (units) {
+      ld_words(vp, wv, pol);
+      ld_words(cp, wc, pol);
+    }
+#pragma unroll 1
+    for (uint32_t u = 0; u < units; u++) {
+      uint32_t nv[NWV], nc[NWC];
+      if (u + 1 < units) {
+        ld_words(vp + S * WS, nv, pol);
+        ld_words(cp + S * WS, nc, pol);
+      }
+#pragma unroll
+      for (int k = 0; k < S; k++)
+        a[k] = fma_acc(Tr<V>::acc(word_val<V>(wv, k)), (Acc)Tr<X>::acc(gather<L1>(x, word_col<C>(wc, k, base))), a[k]);
+#pragma unroll
+      for (int q = 0; q < NWV; q++) wv[q] = nv[q];
+#pragma unroll
+      for (int q = 0; q < NWC; q++) wc[q] = nc[q];
+      vp += S * WS;
+      cp += S * WS;
+    }
+  } else {
 #pragma unroll 2
   for (uint32_t u = 0; u < units; u++) {
     uint32_t wv[NWV], wc[NWC];
@@ -257,6 +314,7 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict_
       a[k] = fma_acc(Tr<V>::acc(word_val<V>(wv, k)), (Acc)Tr<X>::acc(gather<L1>(x, word_col<C>(wc, k, base))), a[k]);
     vp += S * WS;
     cp += S * WS;
+  }
   }
   Acc tail = Acc(0);
   const size_t ut = (size_t)units * S * WS + lane;
@@ -280,11 +338,11 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict_
   return s + tail;
 }
 
-template <typename V, typename X, bool L1>
+template <typename V, typename X, bool L1, bool TUNED = true>
 __device__ __forceinline__ typename Tr<V>::Acc lane_sum_fast(const V *__restrict__ pv, const int32_t *__restrict__ pc,
                                                             int4 d, const X *__restrict__ x, uint32_t lane,
                                                             uint64_t pol) {
-  return lane_sum_vec<V, X, L1, int32_t>(pv, pc + (uint32_t)d.x, 0, d, x, lane, pol);
+  return lane_sum_vec<V, X, L1, int32_t, TUNED>(pv, pc + (uint32_t)d.x, 0, d, x, lane, pol);
 }
 
 // ---- compressed column indices ---------------------------------------------------
@@ -292,14 +350,14 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_fast(const V *__restrict
 // 16-bit offsets from a per-warp base (2 bytes per slot instead of 4); other
 // warps keep 32-bit indices in a compact side array.  cdesc = {base, mode
 // (0 = 16-bit, 1 = 32-bit), offset of the warp in the 32-bit array, 0}.
-template <typename V, typename X, bool L1>
+template <typename V, typename X, bool L1, bool TUNED = true>
 __device__ __forceinline__ typename Tr<V>::Acc lane_sum_compressed(const V *__restrict__ pv,
                                                                   const uint16_t *__restrict__ c16,
                                                                   const int32_t *__restrict__ c32, int4 d,
                                                                   int4 cd, const X *__restrict__ x,
                                                                   uint32_t lane, uint64_t pol) {
-  if (cd.y == 0) return lane_sum_vec<V, X, L1, uint16_t>(pv, c16 + (uint32_t)d.x, cd.x, d, x, lane, pol);
-  return lane_sum_vec<V, X, L1, int32_t>(pv, c32 + (uint32_t)cd.z, 0, d, x, lane, pol);
+  if (cd.y == 0) return lane_sum_vec<V, X, L1, uint16_t, TUNED>(pv, c16 + (uint32_t)d.x, cd.x, d, x, lane, pol);
+  return lane_sum_vec<V, X, L1, int32_t, TUNED>(pv, c32 + (uint32_t)cd.z, 0, d, x, lane, pol);
 }
 
 }  // namespace core
