@@ -451,6 +451,75 @@ def suite_f16s(reps, mesh=96):
             "gbs": round((6 * nnz + 12 * n) / ms / 1e6, 1), "rel_err": err}
 
 
+def _graph_us(fn, launches=100, replays=20):
+    """Microseconds per call of `fn` (stream-ordered launches on the current
+    stream), from CUDA-graph replays of `launches` calls, CUDA events around
+    `replays` replays."""
+    import torch
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        for _ in range(3):
+            fn()
+    torch.cuda.current_stream().wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        for _ in range(launches):
+            fn()
+    for _ in range(3):
+        g.replay()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(replays):
+        g.replay()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) * 1e3 / (replays * launches)
+
+
+def suite_small():
+    """2-D Q1 128^2, 1 dof (16,641 rows, 148,225 nnz, rows of 9/6/4, seed 0),
+    fp64: run (original columns, y scattered through row_map) and run_x
+    (coalesced renumbered columns, reordered x, y in sorted order) for WPK1
+    and WPK2 thresholds 2-8, fast and exact order.  The 2 MB matrix stays in
+    L2, so this reports latency and GFLOP/s (2 flops per nonzero) from
+    CUDA-graph replays, not an HBM fraction."""
+    import numpy as np
+    import torch
+
+    import warpkernel_gb300 as wk
+    from oracle import wk_oracle as O
+    from warpkernel_gb300 import fe
+    rp, cols, vals = fe.fe_matrix(2, 128, 128, 0, 1, 0, 0)
+    n, nnz = rp.numel() - 1, cols.numel()
+    x = fe.uniform_vec(0, 0, n)
+    y_ref = O.csr_spmv(rp.cpu().numpy(), cols.cpu().numpy(), vals.cpu().numpy(), x.cpu().numpy())
+    out = {"workload": "q1_128x128_1dof fp64 seed 0 (L2-resident)", "nrows": n, "nnz": nnz,
+           "timing": "CUDA graph of 100 launches, 20 replays", "layouts": {}}
+    for name, th in (("wpk1", None), ("wpk2_th8", 8), ("wpk2_th5", 5), ("wpk2_th3", 3), ("wpk2_th2", 2)):
+        k = wk.structure().scan(nnz, n, None, rp) if th is None else wk.structure2().scan(nnz, n, None, rp, None, th)
+        e = wk.engine(k, vals, cols)
+        ex = wk.engine(k, vals, cols)
+        ex.device_colinds = k.reorder_columns_coalesced(cols)
+        xr = k.reorder_x(x)
+        y = torch.zeros(n, dtype=torch.float64, device="cuda")
+        yx = torch.zeros(n, dtype=torch.float64, device="cuda")
+        row = {"nwarps": k.nwarps, "allocate_nz": k.allocate_nz}
+        for order, oname in ((0, "fast"), (1, "exact")):
+            us = _graph_us(lambda: e.run(0, 128, x, y, order=order, timed=False))
+            usx = _graph_us(lambda: ex.run_x(0, 128, xr, yx, order=order, timed=False))
+            torch.cuda.synchronize()
+            err = float(np.linalg.norm(y.cpu().numpy() - y_ref) / np.linalg.norm(y_ref))
+            rm = torch.from_numpy(k.row_map.astype(np.int64)).cuda()
+            same = bool(torch.equal(yx, y[rm]))
+            row[oname] = {"run_us": round(us, 2), "run_gflops": round(2 * nnz / us / 1e3, 1),
+                          "run_x_us": round(usx, 2), "run_x_gflops": round(2 * nnz / usx / 1e3, 1),
+                          "rel_err": err, "run_x_equals_run": same}
+        out["layouts"][name] = row
+    return out
+
+
 def suite_batched(count=512, tune=True):
     """512 FE patches (2-D Q1 / 3-D hex, 1k-200k rows, 1 or 3 dof, 1-16 RHS,
     fp32, seed 3) in one persistent CUDA-graph launch; autotuned threshold
@@ -547,7 +616,7 @@ def run_suites(args):
     out = {}
     for name, fn in (("mixed_precision_and_cg", lambda: suite_mixed_and_cg(50)),
                      ("adjoint", lambda: suite_adjoint(50)), ("batched", suite_batched),
-                     ("ablation", lambda: suite_ablation(20))):
+                     ("ablation", lambda: suite_ablation(20)), ("small_q1_128", suite_small)):
         t0 = time.time()
         try:
             out[name] = fn()
@@ -620,7 +689,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-suites", action="store_true",
                     help="skip the mixed-precision / CG / adjoint / batched measurements")
-    ap.add_argument("--only", choices=["mixed", "adjoint", "batched", "ablation", "cg", "f16s"],
+    ap.add_argument("--only", choices=["mixed", "adjoint", "batched", "ablation", "cg", "f16s", "small"],
                     help="run one suite alone (profiling cases; --steps = timed repetitions, "
                          "batched: the first 128 matrices with a fixed threshold / tile)")
     args = ap.parse_args()
@@ -638,6 +707,8 @@ def main():
             res = suite_cg(reps, args.mesh)
         elif args.only == "f16s":
             res = suite_f16s(reps, args.mesh)
+        elif args.only == "small":
+            res = suite_small()
         else:
             res = suite_batched(count=128, tune=False)
         print(json.dumps({"suite": args.only, **res}), flush=True)
