@@ -197,7 +197,8 @@ def run_ours(args):
         torch.cuda.synchronize()
         barrier(world)
     total_ms = max_over_ranks(t0.elapsed_time(t1), world)
-    kern_ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    kern_times = [a.elapsed_time(b) for a, b in ev]
+    kern_ms = statistics.mean(kern_times)
     clocks = clk.summary()
 
     B = alg_bytes(n, nnz)
@@ -260,6 +261,7 @@ def run_ours(args):
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                      "traffic": load_traffic(args.kind, args.threshold),
                      "kernel": "k_spmv_fast<double,MAPPED,L1>", "kernel_ms": round(kern_ms, 5),
+                     "kernel_ms_median": round(statistics.median(kern_times), 5),
                      "alg_bytes_per_launch": B},
     }
     if rank == 0 and not args.no_cpu_baseline:
