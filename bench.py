@@ -429,10 +429,11 @@ def suite_adjoint(reps):
     return out
 
 
-def suite_f16s(reps, mesh=96):
-    """hex mesh^3 (3 dof, seed 2, WPK2 threshold 81): the scaled-FP16
-    (WK_F16S) engine alone, FP32 x and y; GB/s counts 2 B value + 4 B column
-    per nonzero and 4 B x + 4 B y + 4 B row map per row."""
+def suite_f16s(reps, mesh=96, dtype="f16s", cols16=False):
+    """hex mesh^3 (3 dof, seed 2, WPK2 threshold 81): one stored-value engine
+    alone (`dtype` f16s: scaled FP16 values with FP32 x and y; f32; bf16 with
+    bf16 x and FP32 y), optionally with 16-bit columns.  GB/s counts value +
+    column bytes per nonzero and x + y + row map bytes per row."""
     import numpy as np
     import torch
 
@@ -443,14 +444,18 @@ def suite_f16s(reps, mesh=96):
     n, nnz = rp.numel() - 1, cols.numel()
     x = fe.uniform_vec(2, 0, n)
     k = wk.structure2().scan(nnz, n, None, rp, None, 81)
-    e = wk.engine(k, fe.convert(vals, torch.float32), cols, dtype="f16s")
-    xd = x.float()
+    tdt, vb, xb = {"f16s": (torch.float32, 2, 4), "f32": (torch.float32, 4, 4), "bf16": (torch.bfloat16, 2, 2)}[dtype]
+    e = wk.engine(k, fe.convert(vals, tdt), cols, dtype=dtype)
+    if cols16:
+        e.compress_cols()
+    xd = fe.convert(x, tdt)
     yd = torch.zeros(n, dtype=torch.float32, device="cuda")
     ms = _event_ms(lambda: e.run(0, 128, xd, yd, timed=False), reps)
     y_ref = O.csr_spmv(rp.cpu().numpy(), cols.cpu().numpy(), vals.cpu().numpy(), x.cpu().numpy())
     err = float(np.linalg.norm(yd.double().cpu().numpy() - y_ref) / np.linalg.norm(y_ref))
-    return {"workload": f"hex{mesh}_3dof seed 2 f16s", "nrows": n, "nnz": nnz, "ms": round(ms, 4),
-            "gbs": round((6 * nnz + 12 * n) / ms / 1e6, 1), "rel_err": err}
+    ib = 2 if cols16 else 4
+    return {"workload": f"hex{mesh}_3dof seed 2 {dtype}" + ("+cols16" if cols16 else ""), "nrows": n, "nnz": nnz,
+            "ms": round(ms, 4), "gbs": round(((vb + ib) * nnz + (xb + 8) * n) / ms / 1e6, 1), "rel_err": err}
 
 
 def _graph_us(fn, launches=100, replays=20):
@@ -691,6 +696,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-suites", action="store_true",
                     help="skip the mixed-precision / CG / adjoint / batched measurements")
+    ap.add_argument("--value-dtype", choices=["f16s", "f32", "bf16"], default="f16s",
+                    help="--only f16s: the stored value type")
+    ap.add_argument("--cols16", action="store_true", help="--only f16s: 16-bit column storage")
     ap.add_argument("--only", choices=["mixed", "adjoint", "batched", "ablation", "cg", "f16s", "small"],
                     help="run one suite alone (profiling cases; --steps = timed repetitions, "
                          "batched: the first 128 matrices with a fixed threshold / tile)")
@@ -708,7 +716,7 @@ def main():
         elif args.only == "cg":
             res = suite_cg(reps, args.mesh)
         elif args.only == "f16s":
-            res = suite_f16s(reps, args.mesh)
+            res = suite_f16s(reps, args.mesh, args.value_dtype, args.cols16)
         elif args.only == "small":
             res = suite_small()
         else:
