@@ -23,7 +23,7 @@ def torch():
 
 
 def emulate_f16s(L, vals, cols):
-    """Per layout warp: scale 2^(k-15) from the largest magnitude m = f 2^k,
+    """Per layout warp: scale 2^(k-15) from the largest finite magnitude m = f 2^k,
     values / scale rounded to FP16 (nearest even), decoded as FP32 * scale."""
     lay = L.layout
     pv, _ = L.process(vals.astype(np.float32).astype(np.float64), cols)
@@ -33,7 +33,8 @@ def emulate_f16s(L, vals, cols):
     for w in range(lay.nwarps):
         a, b = int(wo[w]), int(wo[w]) + 32 * int(mx[w])
         seg = pv[a:b]
-        m = float(np.max(np.abs(seg))) if b > a else 0.0
+        fin = np.abs(seg[np.isfinite(seg)])
+        m = float(np.max(fin)) if fin.size else 0.0
         e = 0
         if m > 0 and np.isfinite(m):
             e = max(int(np.frexp(np.float32(m))[1]) - 15, -126)
@@ -61,6 +62,25 @@ def test_f16s_values_decode_to_the_emulation(kind, th):
     with O.OracleLayout(rp, kind=kind, threshold=th) as L:
         ref = emulate_f16s(L, vals, cols)
     np.testing.assert_array_equal(eng.device_values.view(np.uint32), ref.view(np.uint32))
+
+
+def test_f16s_non_finite_values_keep_their_warp_scale():
+    """An inf or nan in a layout warp encodes as itself and does not change
+    the scale of the warp's finite values (which would otherwise overflow)."""
+    rng = np.random.default_rng(9)
+    rp, cols, vals = random_csr(rng, 2000, 40, p_empty=0.1)
+    vals = vals * 1e6  # finite values far above FP16's range before scaling
+    vals[::997] = np.inf
+    vals[5::1499] = -np.inf
+    vals[11::1777] = np.nan
+    k, eng = make(1, rp, cols, vals, 0, "f16s")
+    with O.OracleLayout(rp, kind=1) as L:
+        ref = emulate_f16s(L, vals, cols)
+    got = eng.device_values
+    np.testing.assert_array_equal(got, ref)  # nan == nan here; infs keep their sign
+    fin = np.isfinite(ref)
+    assert np.isinf(got[~fin & ~np.isnan(ref)]).all()
+    assert np.abs(got[fin]).max() <= np.abs(vals[np.isfinite(vals)]).max() * 1.001
 
 
 @pytest.mark.parametrize("kind,th", [(1, 0), (2, 5), (2, 81)])

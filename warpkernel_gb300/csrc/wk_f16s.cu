@@ -2,7 +2,7 @@
 // power-of-two scale per layout warp.
 //
 // A layout warp's values share one scale 2^e chosen from the warp's largest
-// magnitude m (m = f * 2^k, f in [0.5, 1), e = k - 15), so m / 2^e lies in
+// finite magnitude m (m = f * 2^k, f in [0.5, 1), e = k - 15), so m / 2^e lies in
 // [2^14, 2^15) below FP16's largest finite value and values up to 2^29 times
 // smaller stay normal.  Dividing by 2^e is exact; the only rounding is FP16's
 // (11-bit significand).  The SpMV kernels sum h * x in FP32 and multiply the
@@ -31,8 +31,11 @@ __global__ void k_f16s_encode(const int4 *__restrict__ desc, uint32_t W, const f
        w += (size_t)gridDim.x * blockDim.x / WS) {
     const int4 d = desc[w];
     const size_t o = (size_t)(uint32_t)d.x, end = o + (size_t)WS * (uint32_t)d.y;
-    float m = 0.f;
-    for (size_t k = o + lane; k < end; k += WS) m = fmaxf(m, fabsf(v32[k]));
+    float m = 0.f;  // largest finite magnitude: inf / nan entries encode as themselves
+    for (size_t k = o + lane; k < end; k += WS) {
+      const float a = fabsf(v32[k]);
+      if (isfinite(a)) m = fmaxf(m, a);
+    }
     for (int s = 16; s > 0; s >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, s));
     int e = 0;
     if (m > 0.f && isfinite(m)) {
