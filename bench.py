@@ -458,6 +458,62 @@ def suite_f16s(reps, mesh=96, dtype="f16s", cols16=False):
             "ms": round(ms, 4), "gbs": round(((vb + ib) * nnz + (xb + 8) * n) / ms / 1e6, 1), "rel_err": err}
 
 
+def suite_permuted(reps, mesh=128):
+    """The headline matrix (hex mesh^3, 3 dof, seed 1) under a seeded random
+    symmetric permutation of rows and columns (A' = P A P^T, columns sorted
+    within rows): the FE locality of the x gathers is gone, x (8 B x n) stays
+    L2-resident.  fp64 WPK2 threshold 81 `run`, algorithmic GB/s (12 B/nnz +
+    20 B/row) beside the unpermuted matrix; y' checked against the
+    unpermuted product under the permutation."""
+    import torch
+
+    import warpkernel_gb300 as wk
+    from warpkernel_gb300 import fe
+    rp, cols, vals = fe.fe_matrix(3, mesh, mesh, mesh, 3, 1, 1)
+    n, nnz = rp.numel() - 1, cols.numel()
+    x = fe.uniform_vec(1, 0, n)
+    out = {"workload": f"hex{mesh}_3dof fp64 seed 1, random symmetric permutation (torch.randperm, seed 1)",
+           "nrows": n, "nnz": nnz}
+
+    def measure(rp_, cols_, vals_, x_):
+        k = wk.structure2().scan(nnz, n, None, rp_, None, 81)
+        e = wk.engine(k, vals_, cols_)
+        y = torch.zeros(n, dtype=torch.float64, device="cuda")
+        ms = _event_ms(lambda: e.run(0, 128, x_, y, timed=False), reps)
+        del e, k
+        return ms, y
+
+    ms0, y0 = measure(rp, cols, vals, x)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(1)
+    perm = torch.randperm(n, device="cuda", generator=g)  # row i of A -> row perm[i] of A'
+    lens = (rp[1:] - rp[:-1]).long()
+    rows = torch.repeat_interleave(torch.arange(n, device="cuda"), lens)
+    key = perm[rows] * n + perm[cols.long()]
+    del rows
+    key, order = torch.sort(key)
+    cols_p = (key % n).to(torch.int32)
+    del key
+    vals_p = vals[order]
+    del order
+    lens_p = torch.empty_like(lens)
+    lens_p[perm] = lens
+    rp_p = torch.zeros(n + 1, dtype=torch.int32, device="cuda")
+    rp_p[1:] = torch.cumsum(lens_p, 0).to(torch.int32)
+    x_p = torch.empty_like(x)
+    x_p[perm] = x
+    del lens, lens_p
+    torch.cuda.empty_cache()
+    ms1, y1 = measure(rp_p, cols_p, vals_p, x_p)
+    err = float((y1[perm] - y0).norm() / y0.norm())
+    B = 12 * nnz + 20 * n
+    out["natural_order"] = {"ms": round(ms0, 4), "gbs": round(B / ms0 / 1e6, 1)}
+    out["permuted"] = {"ms": round(ms1, 4), "gbs": round(B / ms1 / 1e6, 1), "rel_err_vs_natural": err}
+    del rp_p, cols_p, vals_p, x_p, y0, y1, perm
+    torch.cuda.empty_cache()
+    return out
+
+
 def _graph_us(fn, launches=100, replays=20):
     """Microseconds per call of `fn` (stream-ordered launches on the current
     stream), from CUDA-graph replays of `launches` calls, CUDA events around
@@ -623,7 +679,8 @@ def run_suites(args):
     out = {}
     for name, fn in (("mixed_precision_and_cg", lambda: suite_mixed_and_cg(50)),
                      ("adjoint", lambda: suite_adjoint(50)), ("batched", suite_batched),
-                     ("ablation", lambda: suite_ablation(20)), ("small_q1_128", suite_small)):
+                     ("ablation", lambda: suite_ablation(20)), ("small_q1_128", suite_small),
+                     ("permuted_hex128", lambda: suite_permuted(20))):
         t0 = time.time()
         try:
             out[name] = fn()
@@ -699,7 +756,7 @@ def main():
     ap.add_argument("--value-dtype", choices=["f16s", "f32", "bf16"], default="f16s",
                     help="--only f16s: the stored value type")
     ap.add_argument("--cols16", action="store_true", help="--only f16s: 16-bit column storage")
-    ap.add_argument("--only", choices=["mixed", "adjoint", "batched", "ablation", "cg", "f16s", "small"],
+    ap.add_argument("--only", choices=["mixed", "adjoint", "batched", "ablation", "cg", "f16s", "small", "permuted"],
                     help="run one suite alone (profiling cases; --steps = timed repetitions, "
                          "batched: the first 128 matrices with a fixed threshold / tile)")
     args = ap.parse_args()
@@ -719,6 +776,8 @@ def main():
             res = suite_f16s(reps, args.mesh, args.value_dtype, args.cols16)
         elif args.only == "small":
             res = suite_small()
+        elif args.only == "permuted":
+            res = suite_permuted(reps, args.mesh)
         else:
             res = suite_batched(count=128, tune=False)
         print(json.dumps({"suite": args.only, **res}), flush=True)
