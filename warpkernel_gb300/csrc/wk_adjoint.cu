@@ -146,148 +146,17 @@ __global__ void k_dvals(const int4 *__restrict__ desc, uint32_t W, const int32_t
 
 // Fused adjoint for the coinciding layouts of a structurally symmetric A:
 // dx[r] = sum over row r's slots of mirror value * dy[c], and dvals for each
-// slot.  Reads follow the fast SpMV (lane j streams slots 4j..4j+3 of a
-// 4-step unit: layout lanes 4(j%8)+m at step j/8), with one gather of the
-// interleaved (x, dy) pair per slot.  SLOTS: dvals stored at the same slots
-// with one vector store (padding gets 0).  Otherwise (CSR order) the values of
-// a 16-step chunk are staged in shared memory as [layout lane][step] and
-// written segment by segment -- the entries of one layout lane in one chunk
-// are contiguous in CSR order (e = t*A + step), so a half-warp stores 16
-// consecutive values instead of 32 lanes storing 32 scattered ones.
-constexpr int ADJ_WARPS = 8;
-constexpr int ADJ_CHUNK = 16;
-
-template <typename T, bool SLOTS>
-__global__ void __launch_bounds__(ADJ_WARPS * 32) k_adjoint_sym_vec(
-    const int4 *__restrict__ desc, uint32_t W, const int32_t *__restrict__ row_map, const uint32_t *__restrict__ slen,
-    const int32_t *__restrict__ rowptr, uint32_t nzr, uint32_t nrows, const int32_t *__restrict__ pc,
-    const T *__restrict__ tv, const typename Pair<T>::type *__restrict__ xdy, T *__restrict__ dx,
-    T *__restrict__ dvals) {
-  typedef typename Pair<T>::type P;
-  __shared__ T stage[SLOTS ? 1 : ADJ_WARPS][32][ADJ_CHUNK + 1];
-  __shared__ int2 seg[ADJ_WARPS][32];
-  const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
-  if (w < W) {
-    const int4 d = desc[w];
-    const uint32_t T_ = (uint32_t)d.z, A = (uint32_t)d.y, t = lane % T_;
-    const size_t o = (size_t)(uint32_t)d.x;
-    const uint32_t p = (uint32_t)d.w + lane / T_;
-    const bool valid = p < nzr;
-    int32_t row = 0;
-    int kb = 0, el = 0;
-    T dyr = T(0);
-    if (valid) {
-      row = row_map[p];
-      const int len = (int)slen[p];
-      kb = rowptr[row] + (int)(t * A);
-      el = max(0, min((int)A, len - (int)(t * A)));
-      dyr = xdy[row].y;
-    }
-    if (!SLOTS) seg[wib][lane] = make_int2(kb, el);
-    // dy and the real-entry count of the four layout lanes this lane streams
-    T dyv[4];
-    int elv[4];
-#pragma unroll
-    for (int m = 0; m < 4; m++) {
-      dyv[m] = __shfl_sync(0xffffffffu, dyr, (int)(4 * (lane & 7) + m));
-      elv[m] = __shfl_sync(0xffffffffu, el, (int)(4 * (lane & 7) + m));
-    }
-    T acc[4] = {T(0), T(0), T(0), T(0)};
-    T tail = T(0);
-    const uint32_t L0 = 4 * (lane & 7), sl = lane >> 3;
-    for (uint32_t i0 = 0; i0 < A; i0 += ADJ_CHUNK) {
-      const uint32_t i1 = min(i0 + (uint32_t)ADJ_CHUNK, A);
-      uint32_t s = i0;
-      for (; s + 4 <= i1; s += 4) {
-        const size_t base = o + (size_t)s * WS + 4 * lane;
-        const int4 c = __ldcs(reinterpret_cast<const int4 *>(pc + base));
-        T v[4];
-        if constexpr (sizeof(T) == 4) {
-          const float4 f = __ldcs(reinterpret_cast<const float4 *>(tv + base));
-          v[0] = f.x; v[1] = f.y; v[2] = f.z; v[3] = f.w;
-        } else {
-          const double2 a0 = __ldcs(reinterpret_cast<const double2 *>(tv + base));
-          const double2 a1 = __ldcs(reinterpret_cast<const double2 *>(tv + base + 2));
-          v[0] = a0.x; v[1] = a0.y; v[2] = a1.x; v[3] = a1.y;
-        }
-        const int cc[4] = {c.x, c.y, c.z, c.w};
-        const uint32_t step = s + sl;
-        T dv[4];
-#pragma unroll
-        for (int m = 0; m < 4; m++) {
-          const P g = __ldg(xdy + cc[m]);
-          acc[m] = fma(v[m], g.y, acc[m]);
-          dv[m] = (int)step < elv[m] ? dyv[m] * g.x : T(0);
-        }
-        if constexpr (SLOTS) {
-          if constexpr (sizeof(T) == 4) {
-            *reinterpret_cast<float4 *>(dvals + base) = make_float4(dv[0], dv[1], dv[2], dv[3]);
-          } else {
-            *reinterpret_cast<double2 *>(dvals + base) = make_double2(dv[0], dv[1]);
-            *reinterpret_cast<double2 *>(dvals + base + 2) = make_double2(dv[2], dv[3]);
-          }
-        } else {
-#pragma unroll
-          for (int m = 0; m < 4; m++) stage[wib][L0 + m][step - i0] = dv[m];
-        }
-      }
-      for (; s < i1; s++) {  // the last A % 4 steps: one slot per lane
-        const size_t slot = o + (size_t)s * WS + lane;
-        const int c = __ldcs(pc + slot);
-        const P g = __ldg(xdy + c);
-        tail = fma(__ldcs(tv + slot), g.y, tail);
-        const T dv = (int)s < el ? dyr * g.x : T(0);
-        if (SLOTS)
-          dvals[slot] = dv;
-        else
-          stage[SLOTS ? 0 : wib][lane][s - i0] = dv;
-      }
-      if constexpr (!SLOTS) {
-        __syncwarp();
-        const uint32_t nst = i1 - i0, jj = lane & 15;
-#pragma unroll 4
-        for (uint32_t sg = 0; sg < 32; sg += 2) {
-          const uint32_t sgm = sg + (lane >> 4);
-          const int2 si = seg[wib][sgm];
-          const uint32_t e = i0 + jj;
-          if (jj < nst && (int)e < si.y) dvals[(size_t)si.x + e] = stage[wib][sgm][jj];
-        }
-        __syncwarp();
-      }
-    }
-#pragma unroll
-    for (int m = 0; m < 4; m++) {
-      acc[m] += __shfl_xor_sync(0xffffffffu, acc[m], 8);
-      acc[m] += __shfl_xor_sync(0xffffffffu, acc[m], 16);
-    }
-    T s0 = T(0);
-#pragma unroll
-    for (int m = 0; m < 4; m++) {
-      const T tt = __shfl_sync(0xffffffffu, acc[m], (int)(lane >> 2));
-      if ((lane & 3) == (uint32_t)m) s0 = tt;
-    }
-    T total = s0 + tail;
-    for (uint32_t k = 1; k < T_; k <<= 1) total += __shfl_down_sync(0xffffffffu, total, k);
-    if (valid && (lane & (T_ - 1)) == 0) dx[row] = total;
-  }
-  for (size_t q = (size_t)nzr + (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < nrows;
-       q += (size_t)gridDim.x * blockDim.x)
-    dx[row_map[q]] = T(0);
-}
-
-// Fused adjoint, slot order: the streaming pattern of the fast SpMV with S
-// slots per lane (8 for fp32, 4 for fp64: 256-bit loads and stores; measured
-// faster than 4 fp32 slots with 128-bit accesses despite the lower occupancy).
+// slot, with one gather of the interleaved (x, dy) pair per slot.  The
+// streaming pattern is the fast SpMV's with S slots per lane (8 for fp32, 4
+// for fp64: 256-bit loads and stores; measured faster than 4 fp32 slots with
+// 128-bit accesses despite the lower occupancy).  dvals go to the same slots
+// with one vector store per lane, or (CSR order) through shared memory, which
+// measured 11 % faster (fp32) than the 4-slot kernel it replaced.
 template <typename T>
 struct AdjSlots {
   static constexpr int value = core::SlotsPerLane<T>::value;
 };
 #define kAdjS (AdjSlots<T>::value)
-__device__ __forceinline__ void st_words(void *p, const uint32_t (&w)[4]) {
-  asm volatile("st.global.v4.b32 [%0], {%1,%2,%3,%4};" ::"l"(p), "r"(w[0]), "r"(w[1]), "r"(w[2]), "r"(w[3])
-               : "memory");
-}
 __device__ __forceinline__ void st_words(void *p, const uint32_t (&w)[8]) {
   asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "r"(w[0]), "r"(w[1]), "r"(w[2]),
                "r"(w[3]), "r"(w[4]), "r"(w[5]), "r"(w[6]), "r"(w[7])
@@ -302,11 +171,32 @@ __device__ __forceinline__ void put_word(uint32_t *w, int k, double v) {
 // One layout warp of the slot-order adjoint; columns as int32 (C = int32_t)
 // or as 16-bit offsets from `base` (C = uint16_t).  Returns layout lane
 // `lane`'s sum of mirror value * dy[c].
-template <typename T, typename C>
+// CSR: dvals in CSR order.  The gradients of a 16-step chunk are staged in
+// `stg` as [layout lane][step] and written row segment by row segment: the
+// entries of one layout lane in one chunk are contiguous in CSR order
+// (skb[l] + step), so a half-warp stores 16 consecutive values.
+constexpr int ADJ_CSR_CHUNK = 16;
+template <typename T>
+__device__ __forceinline__ void flush_csr_chunk(T *__restrict__ dvals, const T (*stg)[ADJ_CSR_CHUNK + 1],
+                                                const int *__restrict__ skb, const int *__restrict__ sel,
+                                                uint32_t c0, uint32_t nst, uint32_t lane) {
+  __syncwarp();
+  const uint32_t jj = lane & 15;
+#pragma unroll 4
+  for (uint32_t sg = 0; sg < 32; sg += 2) {
+    const uint32_t l = sg + (lane >> 4);
+    const uint32_t e = c0 + jj;
+    if (jj < nst && (int)e < sel[l]) dvals[(size_t)skb[l] + e] = stg[l][jj];
+  }
+  __syncwarp();
+}
+
+template <typename T, typename C, bool CSR>
 __device__ __forceinline__ T adjoint_warp_slots(const int4 d, const C *__restrict__ cp0, int base,
                                                 const T *__restrict__ tv, const typename Pair<T>::type *__restrict__ xdy,
                                                 T *__restrict__ dvals, const T *__restrict__ sdy,
-                                                const int *__restrict__ sel, T dyr, int el,
+                                                const int *__restrict__ sel, const int *__restrict__ skb,
+                                                T (*stg)[ADJ_CSR_CHUNK + 1], T dyr, int el,
                                                 uint32_t lane, uint64_t pol) {
   using namespace core;
   typedef typename Pair<T>::type P;
@@ -338,9 +228,18 @@ __device__ __forceinline__ T adjoint_warp_slots(const int4 d, const C *__restric
       const P g = __ldg(xdy + word_col<C>(wc, m, base));
       acc[m] = fma(word_val<T>(wv, m), g.y, acc[m]);
       const int q = S * (int)(lane % R) + m;
-      put_word(wd, m, step < sel[q] ? sdy[q] * g.x : T(0));
+      const T dv = step < sel[q] ? sdy[q] * g.x : T(0);
+      if constexpr (CSR)
+        stg[q][step % ADJ_CSR_CHUNK] = dv;
+      else
+        put_word(wd, m, dv);
     }
-    st_words(dp, wd);
+    if constexpr (CSR) {
+      if (((u + 1) * S) % ADJ_CSR_CHUNK == 0)
+        flush_csr_chunk(dvals, stg, skb, sel, (u + 1) * S - ADJ_CSR_CHUNK, ADJ_CSR_CHUNK, lane);
+    } else {
+      st_words(dp, wd);
+    }
 #pragma unroll
     for (int q = 0; q < (int)(S * sizeof(T) / 4); q++) wv[q] = nv[q];
 #pragma unroll
@@ -355,7 +254,15 @@ __device__ __forceinline__ T adjoint_warp_slots(const int4 d, const C *__restric
     const size_t k = ut + (size_t)i * WS;
     const P g = __ldg(xdy + ld_col1(cp0 + k, base, pol));
     tail = fma(__ldcs(tv + o + k), g.y, tail);
-    dvals[o + k] = (int)(units * S + i) < el ? dyr * g.x : T(0);
+    const T dv = (int)(units * S + i) < el ? dyr * g.x : T(0);
+    if constexpr (CSR)
+      stg[lane][(units * S + i) % ADJ_CSR_CHUNK] = dv;
+    else
+      dvals[o + k] = dv;
+  }
+  if constexpr (CSR) {  // the last, partial chunk
+    const uint32_t c0 = (units * S / ADJ_CSR_CHUNK) * ADJ_CSR_CHUNK;
+    if (A > c0) flush_csr_chunk(dvals, stg, skb, sel, c0, A - c0, lane);
   }
 #pragma unroll
   for (int mm = R; mm < 32; mm <<= 1) {
@@ -375,16 +282,20 @@ __device__ __forceinline__ T adjoint_warp_slots(const int4 d, const C *__restric
 // flight, and the rows' dy / slot counts read from shared memory instead of
 // held in 16 registers per lane, measured 9 % faster than the first form (76
 // registers, two units unrolled) at hex 64^3, fp32.
-template <typename T, bool COMP>
+// CSR: dvals in CSR order (rowptr gives each row's first entry), staged in
+// shared memory per 16-step chunk.
+template <typename T, bool COMP, bool CSR>
 __global__ void __launch_bounds__(256, 3) k_adjoint_sym_slots(
     const int4 *__restrict__ desc, uint32_t W, const int32_t *__restrict__ row_map, const uint32_t *__restrict__ slen,
-    uint32_t nzr, uint32_t nrows, const int32_t *__restrict__ pc, const uint16_t *__restrict__ c16,
-    const int32_t *__restrict__ c32, const int4 *__restrict__ cdesc, const T *__restrict__ tv,
-    const typename Pair<T>::type *__restrict__ xdy, T *__restrict__ dx, T *__restrict__ dvals) {
+    const int32_t *__restrict__ rowptr, uint32_t nzr, uint32_t nrows, const int32_t *__restrict__ pc,
+    const uint16_t *__restrict__ c16, const int32_t *__restrict__ c32, const int4 *__restrict__ cdesc,
+    const T *__restrict__ tv, const typename Pair<T>::type *__restrict__ xdy, T *__restrict__ dx,
+    T *__restrict__ dvals) {
   using namespace core;
-  constexpr int S = kAdjS, R = 32 / S;
   __shared__ T s_dy[8][32];
   __shared__ int s_el[8][32];
+  __shared__ int s_kb[CSR ? 8 : 1][32];
+  __shared__ T s_stage[CSR ? 8 : 1][32][ADJ_CSR_CHUNK + 1];
   const uint32_t lane = threadIdx.x & 31;
   const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
   if (w < W) {
@@ -394,31 +305,37 @@ __global__ void __launch_bounds__(256, 3) k_adjoint_sym_slots(
     const uint32_t p = (uint32_t)d.w + lane / T_;
     const bool valid = p < nzr;
     int32_t row = 0;
-    int el = 0;
+    int el = 0, kb = 0;
     T dyr = T(0);
     if (valid) {
       row = row_map[p];
       el = max(0, min((int)A, (int)slen[p] - (int)(t * A)));
       dyr = xdy[row].y;
+      if (CSR) kb = rowptr[row] + (int)(t * A);
     }
-    // the warp's 32 row gradients and slot counts, read by the lanes that
-    // store those rows' slots
-    T *sdy = s_dy[threadIdx.x / WS];
-    int *sel = s_el[threadIdx.x / WS];
+    // the warp's 32 row gradients and slot counts (and CSR offsets), read by
+    // the lanes that store those rows' slots
+    const uint32_t wib = threadIdx.x / WS;
+    T *sdy = s_dy[wib];
+    int *sel = s_el[wib];
+    int *skb = s_kb[CSR ? wib : 0];
+    T(*stg)[ADJ_CSR_CHUNK + 1] = s_stage[CSR ? wib : 0];
     sdy[lane] = dyr;
     sel[lane] = el;
+    if (CSR) skb[lane] = kb;
     __syncwarp();
     T total;
     if constexpr (COMP) {
       const int4 cd = cdesc[w];
       if (cd.y == 0)
-        total = adjoint_warp_slots<T, uint16_t>(d, c16 + (uint32_t)d.x, cd.x, tv, xdy, dvals, sdy, sel, dyr, el, lane,
-                                                pol);
+        total = adjoint_warp_slots<T, uint16_t, CSR>(d, c16 + (uint32_t)d.x, cd.x, tv, xdy, dvals, sdy, sel, skb, stg,
+                                                     dyr, el, lane, pol);
       else
-        total = adjoint_warp_slots<T, int32_t>(d, c32 + (uint32_t)cd.z, 0, tv, xdy, dvals, sdy, sel, dyr, el, lane,
-                                               pol);
+        total = adjoint_warp_slots<T, int32_t, CSR>(d, c32 + (uint32_t)cd.z, 0, tv, xdy, dvals, sdy, sel, skb, stg,
+                                                    dyr, el, lane, pol);
     } else {
-      total = adjoint_warp_slots<T, int32_t>(d, pc + (uint32_t)d.x, 0, tv, xdy, dvals, sdy, sel, dyr, el, lane, pol);
+      total = adjoint_warp_slots<T, int32_t, CSR>(d, pc + (uint32_t)d.x, 0, tv, xdy, dvals, sdy, sel, skb, stg, dyr,
+                                                  el, lane, pol);
     }
     for (uint32_t k = 1; k < T_; k <<= 1) total += __shfl_down_sync(0xffffffffu, total, k);
     if (valid && (lane & (T_ - 1)) == 0) dx[row] = total;
@@ -596,34 +513,30 @@ extern "C" wk_status wk_adjoint_run(wk_adjoint *a, const void *x, const void *dy
     const size_t pb = (size_t)n * (f64 ? 16 : 8);
     if (a->xdy.bytes < pb) WK_TRY(a->xdy.alloc(pb));
     const unsigned gi = grid_for(n, 256);
-    const unsigned gv = (unsigned)std::max<size_t>(1, ((size_t)W + ADJ_WARPS - 1) / ADJ_WARPS);
-#define WK_ADJ(T, S)                                                                                                 \
-  k_adjoint_sym_vec<T, S><<<gv, ADJ_WARPS * 32, 0, st>>>(                                                            \
-      L->d.warp_desc, W, L->d.row_map, L->d.slen, L->d.rowptr, L->info.nznrows, n, f->cols.as<int32_t>(),            \
-      a->te->vals.as<T>(), a->xdy.as<typename Pair<T>::type>(), (T *)dx, (T *)dvals)
+#define WK_ADJ_SLOTS1(T, COMP, CSR)                                                                                 \
+  k_adjoint_sym_slots<T, COMP, CSR><<<gs, 256, 0, st>>>(                                                            \
+      L->d.warp_desc, W, L->d.row_map, L->d.slen, L->d.rowptr, L->info.nznrows, n, f->cols.as<int32_t>(),           \
+      f->c16.as<uint16_t>(), f->c32.as<int32_t>(), f->cdesc.as<int4>(), a->te->vals.as<T>(),                        \
+      a->xdy.as<typename Pair<T>::type>(), (T *)dx, (T *)dvals)
 #define WK_ADJ_SLOTS(T)                                                                                             \
   do {                                                                                                              \
     const unsigned gs = (unsigned)std::max<size_t>(1, ((size_t)W + 7) / 8);                                        \
-    if (f->compressed)                                                                                              \
-      k_adjoint_sym_slots<T, true><<<gs, 256, 0, st>>>(                                                             \
-          L->d.warp_desc, W, L->d.row_map, L->d.slen, L->info.nznrows, n, f->cols.as<int32_t>(),                    \
-          f->c16.as<uint16_t>(), f->c32.as<int32_t>(), f->cdesc.as<int4>(), a->te->vals.as<T>(),                    \
-          a->xdy.as<typename Pair<T>::type>(), (T *)dx, (T *)dvals);                                                \
-    else                                                                                                            \
-      k_adjoint_sym_slots<T, false><<<gs, 256, 0, st>>>(                                                            \
-          L->d.warp_desc, W, L->d.row_map, L->d.slen, L->info.nznrows, n, f->cols.as<int32_t>(), nullptr, nullptr,  \
-          nullptr, a->te->vals.as<T>(), a->xdy.as<typename Pair<T>::type>(), (T *)dx, (T *)dvals);                 \
+    if (f->compressed) {                                                                                            \
+      if (slots) WK_ADJ_SLOTS1(T, true, false); else WK_ADJ_SLOTS1(T, true, true);                                  \
+    } else {                                                                                                        \
+      if (slots) WK_ADJ_SLOTS1(T, false, false); else WK_ADJ_SLOTS1(T, false, true);                                \
+    }                                                                                                               \
   } while (0)
     if (slots && ((uintptr_t)dvals & 31u))
       return set_error(WK_ERR_INVALID, "slot-order dvals must be 32-byte aligned");
     if (f64) {
       k_interleave<double><<<gi, 256, 0, st>>>((const double *)x, (const double *)dy, n, a->xdy.as<double2>());
-      if (slots) WK_ADJ_SLOTS(double); else WK_ADJ(double, false);
+      WK_ADJ_SLOTS(double);
     } else {
       k_interleave<float><<<gi, 256, 0, st>>>((const float *)x, (const float *)dy, n, a->xdy.as<float2>());
-      if (slots) WK_ADJ_SLOTS(float); else WK_ADJ(float, false);
+      WK_ADJ_SLOTS(float);
     }
-#undef WK_ADJ
+#undef WK_ADJ_SLOTS1
 #undef WK_ADJ_SLOTS
     WK_CHECK_LAUNCH();
     return WK_OK;
