@@ -298,3 +298,32 @@ def test_fast_order_on_short_warps_is_the_exact_order(dtype):
                 ref = ys[(False, True, 1)].double()
                 rel = float((y.double() - ref).norm() / ref.norm())
                 assert rel < (1e-12 if dtype == "f64" else 1e-5), (dtype, key, rel)
+
+
+def test_run_calls_capture_into_a_cuda_graph():
+    """wk_run / wk_run_x with timed=False are plain stream-ordered launches:
+    captured into a CUDA graph and replayed, they give the bits of direct
+    calls (fast and exact order, WPK1 and WPK2)."""
+    t = torch()
+    rp, cols, vals = O.fe_matrix(2, 40, 40, 0, 1, value_mode=0, seed=0)
+    n = len(rp) - 1
+    for kind, th in ((1, 0), (2, 3)):
+        k, eng = make(kind, rp, cols, vals, th)
+        x = t.from_numpy(O.uniform_vec(0, 0, n)).cuda()
+        for order in (0, 1):
+            direct = t.zeros(n, dtype=t.float64, device="cuda")
+            eng.run(0, 128, x, direct, order=order)
+            y = t.zeros(n, dtype=t.float64, device="cuda")
+            s = t.cuda.Stream()
+            s.wait_stream(t.cuda.current_stream())
+            with t.cuda.stream(s):
+                eng.run(0, 128, x, y, order=order, timed=False)  # warm-up outside capture
+            t.cuda.current_stream().wait_stream(s)
+            g = t.cuda.CUDAGraph()
+            with t.cuda.graph(g):
+                eng.run(0, 128, x, y, order=order, timed=False)
+            y.zero_()
+            for _ in range(3):
+                g.replay()
+            t.cuda.synchronize()
+            assert t.equal(y, direct), (kind, order)
