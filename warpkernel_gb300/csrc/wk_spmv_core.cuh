@@ -25,31 +25,6 @@ __device__ __forceinline__ uint64_t policy_evict_first() {
 }
 
 // ---- streaming loads (matrix), ld.global.nc.L1::no_allocate + evict_first ------
-__device__ __forceinline__ void ld_stream(const double *p, double (&v)[4], uint64_t pol) {
-  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f64 {%0,%1,%2,%3}, [%4], %5;"
-               : "=d"(v[0]), "=d"(v[1]), "=d"(v[2]), "=d"(v[3])
-               : "l"(p), "l"(pol));
-}
-__device__ __forceinline__ void ld_stream(const float *p, float (&v)[4], uint64_t pol) {
-  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f32 {%0,%1,%2,%3}, [%4], %5;"
-               : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3])
-               : "l"(p), "l"(pol));
-}
-__device__ __forceinline__ void ld_stream(const __nv_bfloat16 *p, __nv_bfloat16 (&v)[4], uint64_t pol) {
-  unsigned a, b;
-  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.b32 {%0,%1}, [%2], %3;"
-               : "=r"(a), "=r"(b)
-               : "l"(p), "l"(pol));
-  v[0] = __ushort_as_bfloat16((unsigned short)(a & 0xffffu));
-  v[1] = __ushort_as_bfloat16((unsigned short)(a >> 16));
-  v[2] = __ushort_as_bfloat16((unsigned short)(b & 0xffffu));
-  v[3] = __ushort_as_bfloat16((unsigned short)(b >> 16));
-}
-__device__ __forceinline__ void ld_stream4(const int32_t *p, int (&c)[4], uint64_t pol) {
-  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.s32 {%0,%1,%2,%3}, [%4], %5;"
-               : "=r"(c[0]), "=r"(c[1]), "=r"(c[2]), "=r"(c[3])
-               : "l"(p), "l"(pol));
-}
 template <typename T>
 __device__ __forceinline__ T ld_stream1(const T *p, uint64_t pol);
 template <>
