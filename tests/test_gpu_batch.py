@@ -51,15 +51,25 @@ def test_batch_fp64_and_validation():
     from warpkernel_gb300 import batched
     from warpkernel_gb300._lib import load
     specs = batched.fe_matrix_set(4, seed=2, rows=(1000, 5000))
+    specs[0]["nrhs"] = 16  # a full 16-wide tile
     b = batched.Batch.from_fe(specs, "f64", rhs_tile=2)
     X, Y = batched.make_vectors(specs, torch.float64)
     b.set_vectors(X, Y)
-    b.run()
-    for s, e, x, y in zip(specs, b.engines, X, Y):
+    ref = []
+    for s, e, x in zip(specs, b.engines, X):
+        cols = []
         for j in range(s["nrhs"]):
             yj = torch.zeros(s["nrows"], dtype=torch.float64, device="cuda")
             e.run(0, 128, x[:, j].contiguous(), yj, order=1)
-            assert torch.equal(yj, y[:, j])
+            cols.append(yj)
+        ref.append(torch.stack(cols, 1))
+    for tile in batched.TILES:
+        b.set_tile(tile)
+        for y in Y:
+            y.zero_()
+        b.run()
+        for m, (y, r) in enumerate(zip(Y, ref)):
+            assert torch.equal(y, r), (tile, m)
     assert load().wk_batch_set_tile(b._h, 3) == 1
     h = C.c_void_p()
     nr = np.zeros(1, np.uint32)

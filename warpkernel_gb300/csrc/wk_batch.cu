@@ -84,11 +84,14 @@ __device__ __forceinline__ double staged_val<double>(const uint32_t *sv, int q) 
 // are summed in order (fma from zero), which is the reference's order.
 // Three resident blocks per SM: uncapped, the 16-RHS float kernel takes 117
 // registers (two blocks, 16 warps per SM); capped at 85 it measured 11 % faster.
-#ifndef WK_BATCH_MINB
-#define WK_BATCH_MINB 3
-#endif
+// fp64 with a 16-wide tile (32 registers of accumulators and 32 of gathered
+// X) gets two blocks per SM: capped for three it spilled 336 bytes.
 template <typename T, int TR>
-__global__ void __launch_bounds__(BATCH_BLOCK, WK_BATCH_MINB) k_batch(const BatchMat<T> *__restrict__ mats,
+constexpr int batch_min_blocks() {
+  return sizeof(T) == 8 && TR >= 16 ? 2 : 3;
+}
+template <typename T, int TR>
+__global__ void __launch_bounds__(BATCH_BLOCK, (batch_min_blocks<T, TR>())) k_batch(const BatchMat<T> *__restrict__ mats,
                                                         const int4 *__restrict__ items, uint32_t nitems,
                                                         unsigned *__restrict__ counter) {
   constexpr int S = Unit<T>::S, NWC = Unit<T>::NWC;
