@@ -514,6 +514,61 @@ def suite_permuted(reps, mesh=128):
     return out
 
 
+def suite_setup(mesh=128, host=False):
+    """Layout and engine construction for the headline matrix (hex mesh^3,
+    3 dof, seed 1, WPK2 threshold 81): the device scan (sort, split, offsets,
+    reorder_rows) and the device process (padded values and columns), best of
+    3 after one warm-up, host clock around synchronised calls.  With `host`,
+    the oracle's single-threaded restatement of the reference's host scan and
+    process on the same matrix (what the reference does before every run)."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import warpkernel_gb300 as wk
+    from warpkernel_gb300 import fe
+    rp, cols, vals = fe.fe_matrix(3, mesh, mesh, mesh, 3, 1, 1)
+    n, nnz = rp.numel() - 1, cols.numel()
+
+    def once():
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        k = wk.structure2().scan(nnz, n, None, rp, None, 81)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        e = wk.engine(k, vals, cols)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        del e, k
+        return t1 - t0, t2 - t1
+
+    once()
+    t = [once() for _ in range(3)]
+    out = {"workload": f"hex{mesh}_3dof fp64 seed 1, WPK2 threshold 81", "nrows": n, "nnz": nnz,
+           "device": {"scan_ms": round(min(a for a, _ in t) * 1e3, 2),
+                      "process_ms": round(min(b for _, b in t) * 1e3, 2)}}
+    if host:
+        from oracle import wk_oracle as O
+        rp_h = np.ascontiguousarray(rp.cpu().numpy())
+        cols_h = np.ascontiguousarray(cols.cpu().numpy())
+        vals_h = np.ascontiguousarray(vals.cpu().numpy())
+        L = O.lib()
+        c = O._Layout()
+        t0 = time.perf_counter()
+        rc = L.wko_scan2(rp_h, n, nnz, 81, C.byref(c))
+        t1 = time.perf_counter()
+        if rc == 0:
+            pv = np.zeros(c.allocate_nz, np.float64)
+            pc = np.zeros(c.allocate_nz, np.int32)
+            t2 = time.perf_counter()
+            L.wko_process_f64(C.byref(c), vals_h, cols_h, pv, pc)
+            t3 = time.perf_counter()
+            out["host_oracle_1_thread"] = {"scan_s": round(t1 - t0, 3), "process_s": round(t3 - t2, 3)}
+        L.wko_free(C.byref(c))
+    return out
+
+
 def _graph_us(fn, launches=100, replays=20):
     """Microseconds per call of `fn` (stream-ordered launches on the current
     stream), from CUDA-graph replays of `launches` calls, CUDA events around
@@ -680,7 +735,8 @@ def run_suites(args):
     for name, fn in (("mixed_precision_and_cg", lambda: suite_mixed_and_cg(50)),
                      ("adjoint", lambda: suite_adjoint(50)), ("batched", suite_batched),
                      ("ablation", lambda: suite_ablation(20)), ("small_q1_128", suite_small),
-                     ("permuted_hex128", lambda: suite_permuted(20))):
+                     ("permuted_hex128", lambda: suite_permuted(20)),
+                     ("setup_hex128", suite_setup)):
         t0 = time.time()
         try:
             out[name] = fn()
@@ -756,7 +812,7 @@ def main():
     ap.add_argument("--value-dtype", choices=["f16s", "f32", "bf16"], default="f16s",
                     help="--only f16s: the stored value type")
     ap.add_argument("--cols16", action="store_true", help="--only f16s: 16-bit column storage")
-    ap.add_argument("--only", choices=["mixed", "adjoint", "batched", "ablation", "cg", "f16s", "small", "permuted"],
+    ap.add_argument("--only", choices=["mixed", "adjoint", "batched", "ablation", "cg", "f16s", "small", "permuted", "setup"],
                     help="run one suite alone (profiling cases; --steps = timed repetitions, "
                          "batched: the first 128 matrices with a fixed threshold / tile)")
     args = ap.parse_args()
@@ -778,6 +834,8 @@ def main():
             res = suite_small()
         elif args.only == "permuted":
             res = suite_permuted(reps, args.mesh)
+        elif args.only == "setup":
+            res = suite_setup(args.mesh, host=True)
         else:
             res = suite_batched(count=128, tune=False)
         print(json.dumps({"suite": args.only, **res}), flush=True)
