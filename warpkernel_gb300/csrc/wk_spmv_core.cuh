@@ -201,8 +201,9 @@ __device__ __forceinline__ int ld_col1(const uint16_t *p, int base, uint64_t pol
   return base + (int)v;
 }
 
-// Slots each lane streams per iteration: 32 B of values for fp64 (4 slots),
-// 32 B for fp32 and 16 B for bf16 (8 slots).
+// Base slots per lane and iteration: 32 B of values for fp64 (4 slots), 32 B
+// for fp32 and 16 B for 2-byte values (8 slots).  The adjoint and the CG's
+// SpMV-dot use it as is; VecPlan below adjusts it for wk_run.
 template <typename V>
 struct SlotsPerLane {
   static constexpr int value = sizeof(V) == 8 ? 4 : 8;
