@@ -270,18 +270,7 @@ __device__ __forceinline__ T adjoint_warp_slots(const int4 d, const C *__restric
     const uint32_t c0 = (units * S / ADJ_CSR_CHUNK) * ADJ_CSR_CHUNK;
     if (A > c0) flush_csr_chunk(dvals, stg, skb, sel, c0, A - c0, lane);
   }
-#pragma unroll
-  for (int mm = R; mm < 32; mm <<= 1) {
-#pragma unroll
-    for (int m = 0; m < S; m++) acc[m] += __shfl_xor_sync(0xffffffffu, acc[m], mm);
-  }
-  T s0 = T(0);
-#pragma unroll
-  for (int m = 0; m < S; m++) {
-    const T tt = __shfl_sync(0xffffffffu, acc[m], (int)(lane / S));
-    if (lane % S == (uint32_t)m) s0 = tt;
-  }
-  return s0 + tail;
+  return combine_lanes<S>(acc, lane) + tail;
 }
 
 // Three resident blocks per SM (80 registers) with the next unit's loads in

@@ -230,6 +230,36 @@ struct PlainPlan {
   static constexpr bool pipelined = false;
 };
 
+// Cross-lane combine of the vector path.  Lane j holds S partial sums a[k]
+// for layout lanes S*(j%R)+k (R = 32/S); the S lanes j%R + R*q (q < S) hold
+// the same layout lanes.  Reduce-scatter: in round r the lanes pair across
+// xor distance R<<r, each keeps half of its accumulators and adds its
+// partner's copies of them (the pairs and their order are those of a
+// butterfly over the same distances, so the sums are the same bits), so a
+// lane ends with the total of one layout lane after S-1 additions instead of
+// S*log2(S).  Lane j then holds layout lane S*(j%R) + brev(j/R) (brev over
+// log2(S) bits); one shuffle moves each total to its owning lane.  Returns
+// layout lane `lane`'s total.
+template <int S, typename Acc>
+__device__ __forceinline__ Acc combine_lanes(Acc (&a)[S], uint32_t lane) {
+  constexpr int R = 32 / S;
+  constexpr int LOG = S == 2 ? 1 : S == 4 ? 2 : S == 8 ? 3 : S == 16 ? 4 : 5;
+  static_assert((1 << LOG) == S, "S must be a power of two up to 32");
+#pragma unroll
+  for (int r = 0; r < LOG; r++) {
+    const int n = S >> r, dist = R << r;
+    const bool hi = ((lane / (uint32_t)dist) & 1u) != 0;
+#pragma unroll
+    for (int k = 0; k < n / 2; k++) {
+      const Acc send = hi ? a[k] : a[k + n / 2];
+      const Acc keep = hi ? a[k + n / 2] : a[k];
+      a[k] = keep + __shfl_xor_sync(0xffffffffu, send, dist);
+    }
+  }
+  const uint32_t src = lane / S + R * (__brev(lane % S) >> (32 - LOG));
+  return __shfl_sync(0xffffffffu, a[0], (int)src);
+}
+
 // Fast order: with S slots per lane, a unit of S steps is 32*S consecutive
 // slots; lane j streams slots S*j .. S*j+S-1 (layout lanes S*(j%R) .. +S-1 at
 // step j/R, R = 32/S) with one vector load of values and one of columns.
@@ -298,20 +328,7 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict_
     const int c = ld_col1(cp0 + ut + (size_t)i * WS, base, pol);
     tail = fma_acc(Tr<V>::acc(ld_stream1(pv + o + ut + (size_t)i * WS, pol)), (Acc)Tr<X>::acc(gather<L1>(x, c)), tail);
   }
-#pragma unroll
-  for (int m = R; m < 32; m <<= 1) {
-#pragma unroll
-    for (int k = 0; k < S; k++) a[k] += __shfl_xor_sync(0xffffffffu, a[k], m);
-  }
-  const int src = (int)(lane / S);
-  const uint32_t kk = lane % S;
-  Acc s = Acc(0);
-#pragma unroll
-  for (int k = 0; k < S; k++) {
-    const Acc t = __shfl_sync(0xffffffffu, a[k], src);
-    if (kk == (uint32_t)k) s = t;
-  }
-  return s + tail;
+  return combine_lanes<S>(a, lane) + tail;
 }
 
 template <typename V, typename X, bool L1, bool TUNED = true>
