@@ -259,7 +259,7 @@ def run_ours(args):
         "gpu_launches": args.steps,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                     "traffic": load_traffic(args.kind, args.threshold),
+                     "traffic": load_traffic(args.kind, args.threshold) if args.mesh == 128 else None,
                      "kernel": "k_spmv_fast<double,MAPPED,L1>", "kernel_ms": round(kern_ms, 5),
                      "kernel_ms_median": round(statistics.median(kern_times), 5),
                      "alg_bytes_per_launch": B},
