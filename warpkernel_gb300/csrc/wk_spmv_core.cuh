@@ -264,8 +264,9 @@ __device__ __forceinline__ Acc combine_lanes(Acc (&a)[S], uint32_t lane) {
 // slots; lane j streams slots S*j .. S*j+S-1 (layout lanes S*(j%R) .. +S-1 at
 // step j/R, R = 32/S) with one vector load of values and one of columns.
 // Partials are combined across the S lanes holding the same layout lanes
-// (xor R, 2R, ..., 16) and moved to the owning lane; the A_w % S remaining
-// steps are added one slot per lane.  Returns layout lane `lane`'s total.
+// (combine_lanes) and moved to the owning lane, whose FMA chain then takes
+// the A_w % S remaining steps one slot per lane.  Returns layout lane
+// `lane`'s total.
 // cp0 points at the warp's first column entry (slot o_w of a slot-indexed
 // array, or the warp's start in a compact array); base is added to 16-bit
 // offsets.
@@ -322,13 +323,15 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict_
     cp += S * WS;
   }
   }
-  Acc tail = Acc(0);
+  // the A_w % S remaining steps continue the combined total's FMA chain (no
+  // separate tail sum to add: one FP64 add less per lane on GB300's FP64 pipe)
+  Acc s = combine_lanes<S>(a, lane);
   const size_t ut = (size_t)units * S * WS + lane;
   for (uint32_t i = 0; i < rem; i++) {
     const int c = ld_col1(cp0 + ut + (size_t)i * WS, base, pol);
-    tail = fma_acc(Tr<V>::acc(ld_stream1(pv + o + ut + (size_t)i * WS, pol)), (Acc)Tr<X>::acc(gather<L1>(x, c)), tail);
+    s = fma_acc(Tr<V>::acc(ld_stream1(pv + o + ut + (size_t)i * WS, pol)), (Acc)Tr<X>::acc(gather<L1>(x, c)), s);
   }
-  return combine_lanes<S>(a, lane) + tail;
+  return s;
 }
 
 template <typename V, typename X, bool L1, bool TUNED = true>
