@@ -222,10 +222,11 @@ struct SlotsPerLane {
 template <typename V, typename C>
 struct VecPlan {
   static constexpr int slots = std::is_same<V, __nv_bfloat16>::value ? 16 : SlotsPerLane<V>::value;
-  // units in flight in the plain loop: scaled FP16 with 16-bit columns (4 B
-  // per slot, FP32 x) runs 7 % faster with 4 on two boxes; 4 slowed fp64 by
-  // 6 % and bf16 with 16-bit columns by 2 %, so the others keep 2
-  static constexpr int unroll = (std::is_same<V, __half>::value && sizeof(C) == 2) ? 4 : 2;
+  // units unrolled in the plain loop: scaled FP16 with 16-bit columns (4 B
+  // per slot, FP32 x) runs 7 % faster with 4 on two boxes; fp64 runs 1.3 %
+  // faster with 1 (2 and 3 unrolled units cost registers and 1-6 %); bf16
+  // with 16-bit columns lost 2 % with 4, so the others keep 2
+  static constexpr int unroll = (std::is_same<V, __half>::value && sizeof(C) == 2) ? 4 : sizeof(V) == 8 ? 1 : 2;
   static constexpr bool pipelined = sizeof(V) == 4 && sizeof(C) == 4;
 };
 // The CG's SpMV-dot (FP32 p for every narrow value type, plus the dot
@@ -234,7 +235,7 @@ struct VecPlan {
 template <typename V, typename C>
 struct PlainPlan {
   static constexpr int slots = SlotsPerLane<V>::value;
-  static constexpr int unroll = 2;
+  static constexpr int unroll = sizeof(V) == 8 ? 1 : 2;
   static constexpr bool pipelined = false;
 };
 
