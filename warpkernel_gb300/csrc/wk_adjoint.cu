@@ -277,10 +277,17 @@ __device__ __forceinline__ T adjoint_warp_slots(const int4 d, const C *__restric
 // flight, and the rows' dy / slot counts read from shared memory instead of
 // held in 16 registers per lane, measured 9 % faster than the first form (76
 // registers, two units unrolled) at hex 64^3, fp32.
+// Blocks per SM the registers are capped for: fp64 in slot order runs 4 %
+// faster with four (64 registers); the others measured best with three.
+template <typename T, bool CSR>
+constexpr int adj_min_blocks() {
+  return sizeof(T) == 8 && !CSR ? 4 : 3;
+}
+
 // CSR: dvals in CSR order (rowptr gives each row's first entry), staged in
 // shared memory per chunk of steps.
 template <typename T, bool COMP, bool CSR>
-__global__ void __launch_bounds__(256, 3) k_adjoint_sym_slots(
+__global__ void __launch_bounds__(256, (adj_min_blocks<T, CSR>())) k_adjoint_sym_slots(
     const int4 *__restrict__ desc, uint32_t W, const int32_t *__restrict__ row_map, const uint32_t *__restrict__ slen,
     const int32_t *__restrict__ rowptr, uint32_t nzr, uint32_t nrows, const int32_t *__restrict__ pc,
     const uint16_t *__restrict__ c16, const int32_t *__restrict__ c32, const int4 *__restrict__ cdesc,
