@@ -204,9 +204,13 @@ wk_status wk_engine_destroy(wk_engine *e);
  * the mixed-precision paths): every layout warp whose real entries span fewer
  * than 65,536 columns stores them as 16-bit offsets from a per-warp base, the
  * others keep 32-bit indices in a side array.  Afterwards WK_ORDER_FAST runs
- * stream 2 B instead of 4 B of index per slot; results are bit-identical to
- * the uncompressed fast order.  *wide_warps (optional) = warps left 32-bit.
- * wk_engine_set_colinds rebuilds the compact storage. */
+ * of WK_F32, WK_BF16 and WK_F16S engines stream 2 B instead of 4 B of index
+ * per slot; results are bit-identical to the uncompressed fast order.
+ * WK_F64 engines keep reading 32-bit indices in wk_run / wk_run_x and the CG
+ * (their SpMV is bound by GB300's FP64 rate, and the offsets measured 7 %
+ * slower); the adjoint uses the compact storage for every type.
+ * *wide_warps (optional) = warps left 32-bit.  wk_engine_set_colinds
+ * rebuilds the compact storage. */
 wk_status wk_engine_compress_cols(wk_engine *e, void *stream, uint32_t *wide_warps);
 
 /* ---- SpMV --------------------------------------------------------------- */

@@ -208,7 +208,7 @@ void cg_iteration(const wk_engine *e, const CgVectors<X> &v, double *scal, doubl
   const uint32_t W = l->info.nwarps, n = l->info.nrows;
   const unsigned g = spmv_dot_grid(l);
   const int i_rho = parity ? S_RHO1 : S_RHO0, i_next = parity ? S_RHO0 : S_RHO1;
-  const int mode = short_layout(l, e->dtype) ? 2 : (e->compressed ? 1 : 0);
+  const int mode = short_layout(l, e->dtype) ? 2 : (e->compressed && e->dtype != WK_F64 ? 1 : 0);
 #define WK_SPMV_DOT1(V, M)                                                                                          \
   k_spmv_dot<V, X, M><<<g, CG_BLOCK, 0, st>>>(e->vals.as<V>(), e->cols.as<int32_t>(), e->c16.as<uint16_t>(),      \
                                                  e->c32.as<int32_t>(), e->cdesc.as<int4>(), l->d.warp_desc, W,        \

@@ -138,7 +138,9 @@ wk_status dispatch(const RunArgs &a, unsigned grid, unsigned block) {
   // Fast order on layouts of short warps: the one-slot-per-step kernel beats
   // the vector path's cross-lane combine (short_steps gives the crossovers).
   const bool use_exact = a.order == WK_ORDER_EXACT || short_layout(l, e->dtype);
-  if (e->compressed && !use_exact) {
+  // fp64 keeps 32-bit columns: its SpMV is bound by the FP64 rate, and the
+  // 16-bit offsets (fewer bytes, more integer work) measured 7 % slower
+  if (e->compressed && !use_exact && sizeof(V) < 8) {
     const uint16_t *c16 = e->c16.as<uint16_t>();
     const int32_t *c32 = e->c32.as<int32_t>();
     const int4 *cd = e->cdesc.as<int4>();
