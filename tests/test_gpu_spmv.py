@@ -327,3 +327,41 @@ def test_run_calls_capture_into_a_cuda_graph():
                 g.replay()
             t.cuda.synchronize()
             assert t.equal(y, direct), (kind, order)
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32", "bf16", "f16s"])
+def test_vector_path_warps_of_every_step_count(dtype):
+    """Warps of 1-40 steps among long warps (so the layout takes the vector
+    path for all of them): no unit, exact multiples of the slots per lane
+    (4 / 8 / 16) and every remainder.  Fast order against the exact order of
+    the same engine, within the type's accumulation tolerance, with 32-bit
+    and 16-bit columns."""
+    t = torch()
+    rng = np.random.default_rng(31)
+    lens = [120] * 40 + list(range(1, 41))  # one warp (32 rows) per length
+    n = 32 * len(lens)
+    rp = np.zeros(n + 1, np.int64)
+    rp[1:] = np.cumsum(np.repeat(lens, 32))
+    cols = rng.integers(0, n, int(rp[-1])).astype(np.int32)
+    vals = rng.uniform(-1, 1, int(rp[-1]))
+    rp = rp.astype(np.int32)
+    tdt = {"f64": t.float64, "f32": t.float32, "bf16": t.bfloat16, "f16s": t.float32}[dtype]
+    ydt = t.float64 if dtype == "f64" else t.float32
+    k = wk().structure()
+    k.scan(len(cols), n, None, rp)
+    eng = wk().engine(k, wk().fe.convert(t.from_numpy(vals).cuda(), tdt), t.from_numpy(cols).cuda(), dtype=dtype)
+    x = wk().fe.convert(t.from_numpy(rng.uniform(-1, 1, n)).cuda(), tdt)
+    ys = {}
+    for comp in (False, True):
+        if comp:
+            eng.compress_cols()
+        for order in (0, 1):
+            y = t.zeros(n, dtype=ydt, device="cuda")
+            eng.run(0, 128, x, y, order=order)
+            ys[(comp, order)] = y.double()
+    tol = 1e-13 if dtype == "f64" else 1e-5
+    ref = ys[(False, 1)]
+    for key, y in ys.items():
+        err = (y - ref).abs().max().item() / ref.abs().max().item()
+        assert err < tol, (dtype, key, err)
+    assert t.equal(ys[(True, 0)], ys[(False, 0)])  # 16-bit columns: the same sums
