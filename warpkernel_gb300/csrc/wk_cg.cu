@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(CG_BLOCK) k_spmv_dot(const V *__restrict__ pv,
                                                        const double *__restrict__ scal, double *__restrict__ partials,
                                                        const float *__restrict__ wscale) {
   if (done(scal)) return;
-  __shared__ double sh[32];
+  __shared__ double sh[CG_BLOCK];
   const uint32_t lane = threadIdx.x & 31;
   double part = 0.0;
   const uint64_t pol = policy_evict_first();
@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(CG_BLOCK) k_spmv_dot(const V *__restrict__ pv,
   for (size_t k = (size_t)nzr + (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nrows;
        k += (size_t)gridDim.x * blockDim.x)
     q[row_map[k]] = X(0);
-  const double t = block_sum(part, sh);
+  const double t = block_sum_staged<CG_BLOCK>(part, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = t;
 }
 

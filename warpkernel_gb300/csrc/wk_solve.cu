@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(RES_BLOCK) k_residual(const double *__restrict
                                                         uint32_t nrows, const double *__restrict__ x,
                                                         const double *__restrict__ b, double *__restrict__ r,
                                                         double *__restrict__ partials) {
-  __shared__ double sh[32];
+  __shared__ double sh[RES_BLOCK];
   const uint32_t lane = threadIdx.x & 31;
   const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
   double part = 0.0;
@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(RES_BLOCK) k_residual(const double *__restrict
     r[row] = bb;
     part = fma(bb, bb, part);
   }
-  const double t = block_sum(part, sh);
+  const double t = block_sum_staged<RES_BLOCK>(part, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = t;
 }
 

@@ -269,6 +269,28 @@ __device__ __forceinline__ Acc combine_lanes(Acc (&a)[S], uint32_t lane) {
   return __shfl_sync(0xffffffffu, a[0], (int)src);
 }
 
+// Block sum of one double per thread for kernels that share GB300's FP64
+// pipe with their DFMAs: the values go to shared memory (sh: NT doubles) and
+// warp 0 adds NT / 32 of them per lane, then a shuffle tree -- 3 + 5 FP64
+// warp instructions for NT = 128 instead of 25 for a tree in every warp (the
+// per-warp trees cost 5 % of a CG iteration at hex 96^3).  Fixed order; the
+// result is valid in thread 0.
+template <int NT>
+__device__ __forceinline__ double block_sum_staged(double v, double *sh) {
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    t = sh[lane];
+#pragma unroll
+    for (int k = 1; k < NT / 32; k++) t += sh[lane + 32 * k];
+#pragma unroll
+    for (int off = 16; off; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+  }
+  return t;
+}
+
 // Fast order: with S slots per lane, a unit of S steps is 32*S consecutive
 // slots; lane j streams slots S*j .. S*j+S-1 (layout lanes S*(j%R) .. +S-1 at
 // step j/R, R = 32/S) with one vector load of values and one of columns.
@@ -286,7 +308,6 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict_
   typedef typename Tr<V>::Acc Acc;
   typedef typename std::conditional<TUNED, VecPlan<V, C>, PlainPlan<V, C>>::type Plan;
   constexpr int S = Plan::slots;
-  constexpr int R = 32 / S;
   constexpr int NWV = S * (int)sizeof(V) / 4, NWC = S * (int)sizeof(C) / 4;
   const uint32_t A = (uint32_t)d.y;
   const size_t o = (size_t)(uint32_t)d.x;
