@@ -68,7 +68,10 @@ __global__ void __launch_bounds__(CG_BLOCK) k_spmv_dot(const V *__restrict__ pv,
   if (done(scal)) return;
   __shared__ double sh[CG_BLOCK];
   const uint32_t lane = threadIdx.x & 31;
-  double part = 0.0;
+  // p . q in the vectors' precision: FP64, or FP32 for the inner solve
+  // (no float <-> double conversions per row on GB300's FP64 pipe)
+  typedef typename std::conditional<sizeof(X) == 8, double, float>::type D;
+  D part = D(0);
   const uint64_t pol = policy_evict_first();
   const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
   if (w < W) {
@@ -88,14 +91,14 @@ __global__ void __launch_bounds__(CG_BLOCK) k_spmv_dot(const V *__restrict__ pv,
       const int32_t row = row_map[r];
       const X qv = (X)s;
       q[row] = qv;
-      part = fma((double)p[row], (double)qv, part);
+      part = fma((D)p[row], (D)qv, part);
     }
   }
   for (size_t k = (size_t)nzr + (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nrows;
        k += (size_t)gridDim.x * blockDim.x)
     q[row_map[k]] = X(0);
-  const double t = block_sum_staged<CG_BLOCK>(part, sh);
-  if (threadIdx.x == 0) partials[blockIdx.x] = t;
+  const D t = block_sum_staged<CG_BLOCK, D>(part, reinterpret_cast<D *>(sh));
+  if (threadIdx.x == 0) partials[blockIdx.x] = (double)t;
 }
 
 // scal[out] = fixed-order sum of partials[0..n); with CHECK also counts the
@@ -121,22 +124,38 @@ __global__ void __launch_bounds__(1024) k_finish(const double *__restrict__ part
   }
 }
 
-// x += alpha p, r -= alpha q, partials of r . r; alpha = scal[rho] / scal[pq]
+// x += alpha p, r -= alpha q, partials of r . r; alpha = scal[rho] / scal[pq].
+// FP32 vectors (the inner solve of IR-CG, whose tolerance is loose) are
+// updated in FP32 arithmetic with each thread's r . r accumulated in FP32:
+// on GB300 the float <-> double conversions of an FP64 update run at the
+// FP64 rate and made these vector kernels FP64-bound.
 template <typename T>
 __global__ void __launch_bounds__(VEC_BLOCK) k_update(T *__restrict__ x, T *__restrict__ r, const T *__restrict__ p,
                                                       const T *__restrict__ q, uint32_t n, const double *__restrict__ scal,
                                                       int i_rho, double *__restrict__ partials) {
   if (done(scal)) return;
-  __shared__ double sh[32];
+  __shared__ double sh[VEC_BLOCK];
   const double alpha = safe_div(scal[i_rho], scal[S_PQ]);
   double part = 0.0;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const T ri = (T)((double)r[i] - alpha * (double)q[i]);
-    x[i] = (T)((double)x[i] + alpha * (double)p[i]);
-    r[i] = ri;
-    part = fma((double)ri, (double)ri, part);
+  if constexpr (sizeof(T) == 8) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+      const T ri = r[i] - alpha * q[i];
+      x[i] = x[i] + alpha * p[i];
+      r[i] = ri;
+      part = fma(ri, ri, part);
+    }
+  } else {
+    const float a = (float)alpha;
+    float part32 = 0.f;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+      const float ri = r[i] - a * q[i];
+      x[i] = x[i] + a * p[i];
+      r[i] = ri;
+      part32 = fmaf(ri, ri, part32);
+    }
+    part = (double)part32;
   }
-  const double t = block_sum(part, sh);
+  const double t = block_sum_staged<VEC_BLOCK>(part, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = t;
 }
 
@@ -146,8 +165,9 @@ __global__ void __launch_bounds__(VEC_BLOCK) k_pupdate(T *__restrict__ p, const 
                                                        const double *__restrict__ scal, int i_rr, int i_rho) {
   if (done(scal)) return;
   const double beta = safe_div(scal[i_rr], scal[i_rho]);
+  const T b = (T)beta;  // FP32 vectors: FP32 arithmetic (see k_update)
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    p[i] = (T)((double)r[i] + beta * (double)p[i]);
+    p[i] = r[i] + b * p[i];
 }
 
 template <typename T>

@@ -269,17 +269,17 @@ __device__ __forceinline__ Acc combine_lanes(Acc (&a)[S], uint32_t lane) {
   return __shfl_sync(0xffffffffu, a[0], (int)src);
 }
 
-// Block sum of one double per thread for kernels that share GB300's FP64
-// pipe with their DFMAs: the values go to shared memory (sh: NT doubles) and
+// Block sum of one value per thread for kernels that share GB300's FP64
+// pipe with their DFMAs: the values go to shared memory (sh: NT values) and
 // warp 0 adds NT / 32 of them per lane, then a shuffle tree -- 3 + 5 FP64
 // warp instructions for NT = 128 instead of 25 for a tree in every warp (the
 // per-warp trees cost 5 % of a CG iteration at hex 96^3).  Fixed order; the
 // result is valid in thread 0.
-template <int NT>
-__device__ __forceinline__ double block_sum_staged(double v, double *sh) {
+template <int NT, typename T = double>
+__device__ __forceinline__ T block_sum_staged(T v, T *sh) {
   sh[threadIdx.x] = v;
   __syncthreads();
-  double t = 0.0;
+  T t = T(0);
   if (threadIdx.x < 32) {
     const int lane = threadIdx.x;
     t = sh[lane];
