@@ -361,8 +361,10 @@ wk_status wk_cg(wk_engine *e, const double *b, double *x, wk_cg_params *p, void 
 /* Iterative-refinement CG: the residual b - A x, its norm, the dot products of
  * the outer loop and the update x += d stay fp64 (engine e64); each
  * correction d solves A d = r with an fp32 CG on the low-precision engine `lo`
- * (WK_F32 or WK_BF16 values, fp32 vectors, compressed columns if
- * wk_engine_compress_cols was called). */
+ * (WK_F32, WK_BF16 or WK_F16S values, compressed columns if
+ * wk_engine_compress_cols was called): fp32 vectors updated in fp32
+ * arithmetic, dot products summed in fp32 within a block and in fp64 across
+ * blocks. */
 wk_status wk_ir_cg(wk_engine *e64, wk_engine *lo, const double *b, double *x, wk_cg_params *p,
                    void *stream);
 
