@@ -170,14 +170,16 @@ __global__ void __launch_bounds__(VEC_BLOCK) k_pupdate(T *__restrict__ p, const 
     p[i] = r[i] + b * p[i];
 }
 
+// partials of a . a, each thread's share in the vector's precision (see
+// k_update), the block sum in fp64
 template <typename T>
 __global__ void __launch_bounds__(VEC_BLOCK) k_dot_self(const T *__restrict__ a, uint32_t n,
                                                         double *__restrict__ partials) {
-  __shared__ double sh[32];
-  double part = 0.0;
+  __shared__ double sh[VEC_BLOCK];
+  T part = T(0);
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    part = fma((double)a[i], (double)a[i], part);
-  const double t = block_sum(part, sh);
+    part = fma(a[i], a[i], part);
+  const double t = block_sum_staged<VEC_BLOCK>((double)part, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = t;
 }
 
