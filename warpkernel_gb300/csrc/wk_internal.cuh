@@ -123,6 +123,7 @@ struct wk_layout {
   // Slot-weighted mean of the warps' step counts (sum A_w^2 / sum A_w): the
   // fast order runs the one-slot-per-step kernel when it is small.
   double mean_steps = 0.0;
+  double sum_steps = 0.0, max_steps = 0.0;  // sum and max of A_w over the warps
 };
 
 struct wk_engine {
@@ -219,6 +220,11 @@ inline double short_steps(int dtype) {
   }
 }
 inline bool short_layout(const wk_layout *l, int dtype) { return l->mean_steps < short_steps(dtype); }
+// True if the longest warp alone outlasts the rest of the work: its steps
+// times the warps the GPU keeps resident (152 SMs x 32) exceed all warps'
+// steps together (a WPK1 layout of a power-law matrix: a few hundred warps of
+// 2,000 steps).  Each such warp's own loads in flight then set the time.
+inline bool long_warps(const wk_layout *l) { return l->max_steps * (152.0 * 32.0) > l->sum_steps; }
 // Grid / block of a one-warp-per-layout-warp launch (nblocks/blocksize <= 0: automatic).
 wk_status launch_shape(uint32_t W, int nblocks, int blocksize, unsigned *grid, unsigned *block);
 

@@ -321,20 +321,25 @@ __global__ void k_warp_tail(int32_t *warp_offsets, uint32_t *row_off, uint32_t W
   if (wpk2) row_off[W] = nrows;
 }
 
+// m[0] += sum A_w^2, m[1] += sum A_w, m[2] = max A_w (exact, any order).
 __global__ void k_step_moments(const uint32_t *__restrict__ steps, uint32_t W, unsigned long long *__restrict__ m) {
-  unsigned long long a2 = 0, a1 = 0;
+  unsigned long long a2 = 0, a1 = 0, am = 0;
   for (size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x; w < W; w += (size_t)gridDim.x * blockDim.x) {
     const unsigned long long a = steps[w];
     a2 += a * a;
     a1 += a;
+    am = a > am ? a : am;
   }
   for (int o = 16; o; o >>= 1) {
     a2 += __shfl_xor_sync(0xffffffffu, a2, o);
     a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+    const unsigned long long b = __shfl_xor_sync(0xffffffffu, am, o);
+    am = b > am ? b : am;
   }
   if ((threadIdx.x & 31) == 0 && a1) {
     atomicAdd(m, a2);
     atomicAdd(m + 1, a1);
+    atomicMax(m + 2, am);
   }
 }
 
@@ -533,7 +538,7 @@ wk_status build_layout(wk_layout *l, const int32_t *d_rowptr, int kind, int32_t 
   WK_TRY(wsb.alloc((size_t)W0 * sizeof(WarpSplit)));
   WK_TRY(cnt.alloc((size_t)W0 * 8));
   WK_TRY(slots.alloc((size_t)W0 * 8));
-  WK_TRY(tot.alloc(2 * 8));
+  WK_TRY(tot.alloc(3 * 8));
   auto *totals = tot.as<unsigned long long>();
   if (W0) {
     k_warp_split<<<grid_for(W0, 256), 256, 0, st>>>(d.slen, nzr, W0, (uint32_t)threshold, wpk2, nosort,
@@ -586,14 +591,16 @@ wk_status build_layout(wk_layout *l, const int32_t *d_rowptr, int kind, int32_t 
   }
   k_warp_tail<<<1, 1, 0, st>>>(d.warp_offsets, d.row_offset_warp, W, n, totals + 1, wpk2);
   WK_CHECK_LAUNCH();
-  if (W) {  // sum A_w^2 and sum A_w (exact integer sums, any order)
-    WK_CUDA(cudaMemsetAsync(tot.p, 0, 16, st));
+  if (W) {  // sum A_w^2, sum A_w and max A_w (exact integers, any order)
+    WK_CUDA(cudaMemsetAsync(tot.p, 0, 24, st));
     k_step_moments<<<grid_for(W, 256), 256, 0, st>>>(d.max_nz_rows, W, totals);
     WK_CHECK_LAUNCH();
-    unsigned long long hm[2];
+    unsigned long long hm[3];
     WK_CUDA(cudaMemcpyAsync(hm, totals, sizeof hm, cudaMemcpyDeviceToHost, st));
     WK_CUDA(cudaStreamSynchronize(st));
     l->mean_steps = hm[1] ? (double)hm[0] / (double)hm[1] : 0.0;
+    l->sum_steps = (double)hm[1];
+    l->max_steps = (double)hm[2];
   }
 
   // 5. reorder_rows

@@ -46,7 +46,9 @@ __global__ void __launch_bounds__(1024) k_spmv_exact(const V *__restrict__ pv, c
   if (valid && (lane & (T - 1)) == 0) store_row<typename Tr<V>::Acc, MAPPED>(y, row_map, p, s);
 }
 
-template <typename V, typename X, bool MAPPED, bool L1>
+// UNR: unroll factor replacing the plan's (0: the plan's), for layouts of
+// long warps (long_warps): fp64 takes 2 there.
+template <typename V, typename X, bool MAPPED, bool L1, int UNR = 0>
 __global__ void __launch_bounds__(1024) k_spmv_fast(const V *__restrict__ pv, const int32_t *__restrict__ pc,
                                                     const int4 *__restrict__ desc, uint32_t W,
                                                     const int32_t *__restrict__ row_map, uint32_t nzr,
@@ -57,7 +59,7 @@ __global__ void __launch_bounds__(1024) k_spmv_fast(const V *__restrict__ pv, co
   if (w >= W) return;
   const int4 d = desc[w];
   const uint32_t T = (uint32_t)d.z;
-  typename Tr<V>::Acc s = lane_sum_fast<V, X, L1>(pv, pc, d, x, lane, policy_evict_first());
+  typename Tr<V>::Acc s = lane_sum_fast<V, X, L1, true, UNR>(pv, pc, d, x, lane, policy_evict_first());
   const uint32_t p = (uint32_t)d.w + lane / T;
   s = row_tree(s, T);
   if constexpr (Scaled<V>::value) s *= wscale[w];
@@ -160,6 +162,17 @@ wk_status dispatch(const RunArgs &a, unsigned grid, unsigned block) {
     } else {
       if (c) WK_LAUNCH(k_spmv_exact, false, true); else WK_LAUNCH(k_spmv_exact, false, false);
     }
+  } else if (sizeof(V) == 8 && long_warps(l)) {
+    // fp64 runs its unit loop without unrolling (fewer registers, 1.3 % faster
+    // on FE layouts); a layout whose longest warps set the time keeps two
+    // units in flight per warp (power-law WPK1, 1 M rows: 0.57 -> 0.43 ms)
+#define WK_LAUNCH2(M, C) k_spmv_fast<V, X, M, C, 2><<<grid, block, 0, a.stream>>>(pv, pc, desc, W, rm, nzr, x, y, ws)
+    if (a.mapped) {
+      if (c) WK_LAUNCH2(true, true); else WK_LAUNCH2(true, false);
+    } else {
+      if (c) WK_LAUNCH2(false, true); else WK_LAUNCH2(false, false);
+    }
+#undef WK_LAUNCH2
   } else {
     if (a.mapped) {
       if (c) WK_LAUNCH(k_spmv_fast, true, true); else WK_LAUNCH(k_spmv_fast, true, false);

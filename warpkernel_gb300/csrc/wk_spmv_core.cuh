@@ -301,7 +301,8 @@ __device__ __forceinline__ T block_sum_staged(T v, T *sh) {
 // cp0 points at the warp's first column entry (slot o_w of a slot-indexed
 // array, or the warp's start in a compact array); base is added to 16-bit
 // offsets.
-template <typename V, typename X, bool L1, typename C, bool TUNED = true>
+// UNR (if non-zero) replaces the plan's unroll factor.
+template <typename V, typename X, bool L1, typename C, bool TUNED = true, int UNR = 0>
 __device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict__ pv, const C *__restrict__ cp0, int base,
                                                            int4 d, const X *__restrict__ x, uint32_t lane,
                                                            uint64_t pol) {
@@ -341,7 +342,8 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict_
       cp += S * WS;
     }
   } else {
-#pragma unroll Plan::unroll
+    constexpr int U = UNR ? UNR : Plan::unroll;
+#pragma unroll U
   for (uint32_t u = 0; u < units; u++) {
     uint32_t wv[NWV], wc[NWC];
     ld_words(vp, wv, pol);
@@ -354,21 +356,44 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict_
   }
   }
   // the A_w % S remaining steps continue the combined total's FMA chain (no
-  // separate tail sum to add: one FP64 add less per lane on GB300's FP64 pipe)
-  Acc s = combine_lanes<S>(a, lane);
+  // separate tail sum to add: one FP64 add less per lane on GB300's FP64
+  // pipe).  With 4 slots per lane (fp64) their operands are loaded before the
+  // combine, whose shuffles then overlap the loads: loading them after it
+  // made layouts of long warps 15 % slower; with 8 slots the 14 preloaded
+  // registers made scaled FP16 with 16-bit columns 10 % slower.
   const size_t ut = (size_t)units * S * WS + lane;
-  for (uint32_t i = 0; i < rem; i++) {
-    const int c = ld_col1(cp0 + ut + (size_t)i * WS, base, pol);
-    s = fma_acc(Tr<V>::acc(ld_stream1(pv + o + ut + (size_t)i * WS, pol)), (Acc)Tr<X>::acc(gather<L1>(x, c)), s);
+  if constexpr (S <= 4) {
+    Acc tv[S - 1], tx[S - 1];
+#pragma unroll
+    for (int i = 0; i < S - 1; i++) {
+      tv[i] = Acc(0);
+      tx[i] = Acc(0);
+      if ((uint32_t)i < rem) {
+        const size_t k = ut + (size_t)i * WS;
+        tv[i] = Tr<V>::acc(ld_stream1(pv + o + k, pol));
+        tx[i] = (Acc)Tr<X>::acc(gather<L1>(x, ld_col1(cp0 + k, base, pol)));
+      }
+    }
+    Acc s = combine_lanes<S>(a, lane);
+#pragma unroll
+    for (int i = 0; i < S - 1; i++)
+      if ((uint32_t)i < rem) s = fma_acc(tv[i], tx[i], s);
+    return s;
+  } else {
+    Acc s = combine_lanes<S>(a, lane);
+    for (uint32_t i = 0; i < rem; i++) {
+      const int c = ld_col1(cp0 + ut + (size_t)i * WS, base, pol);
+      s = fma_acc(Tr<V>::acc(ld_stream1(pv + o + ut + (size_t)i * WS, pol)), (Acc)Tr<X>::acc(gather<L1>(x, c)), s);
+    }
+    return s;
   }
-  return s;
 }
 
-template <typename V, typename X, bool L1, bool TUNED = true>
+template <typename V, typename X, bool L1, bool TUNED = true, int UNR = 0>
 __device__ __forceinline__ typename Tr<V>::Acc lane_sum_fast(const V *__restrict__ pv, const int32_t *__restrict__ pc,
                                                             int4 d, const X *__restrict__ x, uint32_t lane,
                                                             uint64_t pol) {
-  return lane_sum_vec<V, X, L1, int32_t, TUNED>(pv, pc + (uint32_t)d.x, 0, d, x, lane, pol);
+  return lane_sum_vec<V, X, L1, int32_t, TUNED, UNR>(pv, pc + (uint32_t)d.x, 0, d, x, lane, pol);
 }
 
 // ---- compressed column indices ---------------------------------------------------
