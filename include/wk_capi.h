@@ -221,7 +221,7 @@ enum {
   WK_ORDER_EXACT = 1  /* the reference's order, bit-identical to the oracle  */
 };
 /* WK_ORDER_FAST on a layout of short warps (slot-weighted mean step count
- * below 48 for fp64, 20 for fp32 and bf16, 16 for scaled FP16) runs the exact-order
+ * below 32 for fp64, 20 for fp32 and bf16, 16 for scaled FP16) runs the exact-order
  * kernel, which is the faster one there; its results then equal
  * WK_ORDER_EXACT's and compressed columns are not used. */
 

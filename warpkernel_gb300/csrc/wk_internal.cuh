@@ -208,12 +208,12 @@ wk_status launch_spmv(const RunArgs &a);
 // True if the layout's warps are short for `dtype`: the one-slot-per-step
 // loop then beats the vector path.  Crossovers of the slot-weighted mean step
 // count measured on hex meshes (1-3 dof, WPK2 thresholds giving 6-81 steps):
-// fp64 between 41 and 54 steps, fp32 and bf16 near 25 with 32-bit columns and
-// near 17 with 16-bit ones, scaled FP16 near 10.  One value per type keeps
+// fp64 between 27 and 41 steps (vector / exact time 0.97-1.09 at 27, 0.97 at
+// 41), fp32 and bf16 near 21, scaled FP16 near 10.  One value per type keeps
 // the 16-bit column form's sums bit-identical to the 32-bit form's.
 inline double short_steps(int dtype) {
   switch (dtype) {
-    case WK_F64: return 48.0;
+    case WK_F64: return 32.0;
     case WK_F32:
     case WK_BF16: return 20.0;
     default: return 16.0;
