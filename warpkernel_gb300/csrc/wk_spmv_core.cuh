@@ -224,14 +224,17 @@ struct VecPlan {
   static constexpr int slots = std::is_same<V, __nv_bfloat16>::value ? 16 : SlotsPerLane<V>::value;
   // units unrolled in the plain loop: scaled FP16 with 16-bit columns (4 B
   // per slot, FP32 x) runs 7 % faster with 4 on two boxes; fp64 runs 1.3 %
-  // faster with 1 (2 and 3 unrolled units cost registers and 1-6 %); bf16
-  // with 16-bit columns lost 2 % with 4, so the others keep 2
+  // faster with 1 (2 and 3 unrolled units cost registers and 1-6 %) except on
+  // layouts of long warps, where k_spmv_fast overrides it with 2; bf16 with
+  // 16-bit columns lost 2 % with 4, so the others keep 2
   static constexpr int unroll = (std::is_same<V, __half>::value && sizeof(C) == 2) ? 4 : sizeof(V) == 8 ? 1 : 2;
   static constexpr bool pipelined = sizeof(V) == 4 && sizeof(C) == 4;
 };
 // The CG's SpMV-dot (FP32 p for every narrow value type, plus the dot
-// product) keeps 8 slots and the plain loop: the plan above raised its
-// registers from 40-48 to 64 and slowed the FP32 / bf16 inner solves by 4 %.
+// product) keeps the base slot count and the plain loop: the plan above
+// raised its registers from 40-48 to 64 and slowed the FP32 / bf16 inner
+// solves by 4 %.  fp64 runs without unrolling, as above (1.4 % per CG
+// iteration).
 template <typename V, typename C>
 struct PlainPlan {
   static constexpr int slots = SlotsPerLane<V>::value;
