@@ -157,9 +157,13 @@ struct AdjSlots {
   static constexpr int value = core::SlotsPerLane<T>::value;
 };
 #define kAdjS (AdjSlots<T>::value)
-__device__ __forceinline__ void st_words(void *p, const uint32_t (&w)[8]) {
-  asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "r"(w[0]), "r"(w[1]), "r"(w[2]),
-               "r"(w[3]), "r"(w[4]), "r"(w[5]), "r"(w[6]), "r"(w[7])
+// dvals are written once and not read again by the kernel: evict-first in L2
+// (and streaming stores in the tail and the CSR flush), so they do not
+// displace the gathered (x, dy) pairs -- 5 % faster in slot order, 8 % with
+// 16-bit columns, fp32 hex 64^3.
+__device__ __forceinline__ void st_words(void *p, const uint32_t (&w)[8], uint64_t pol) {
+  asm volatile("st.global.L1::no_allocate.L2::cache_hint.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8}, %9;" ::"l"(p),
+               "r"(w[0]), "r"(w[1]), "r"(w[2]), "r"(w[3]), "r"(w[4]), "r"(w[5]), "r"(w[6]), "r"(w[7]), "l"(pol)
                : "memory");
 }
 __device__ __forceinline__ void put_word(uint32_t *w, int k, float v) { w[k] = __float_as_uint(v); }
@@ -192,12 +196,12 @@ __device__ __forceinline__ void flush_csr_chunk(T *__restrict__ dvals, const T (
   for (uint32_t sg = 0; sg < 32; sg += 32 / ADJ_CSR_CHUNK) {
     const uint32_t l = sg + lane / ADJ_CSR_CHUNK;
     const uint32_t e = c0 + jj;
-    if (jj < nst && (int)e < sel[l]) dvals[(size_t)skb[l] + e] = stg[l][jj];
+    if (jj < nst && (int)e < sel[l]) __stcs(dvals + (size_t)skb[l] + e, stg[l][jj]);
   }
   __syncwarp();
 }
 
-template <typename T, typename C, bool CSR>
+template <typename T, typename C, bool CSR, int DEPTH>
 __device__ __forceinline__ T adjoint_warp_slots(const int4 d, const C *__restrict__ cp0, int base,
                                                 const T *__restrict__ tv, const typename Pair<T>::type *__restrict__ xdy,
                                                 T *__restrict__ dvals, const T *__restrict__ sdy,
@@ -216,23 +220,28 @@ __device__ __forceinline__ T adjoint_warp_slots(const int4 d, const C *__restric
   const T *vp = tv + o + S * lane;
   const C *cp = cp0 + S * lane;
   T *dp = dvals + o + S * lane;
-  uint32_t wv[S * sizeof(T) / 4], wc[S * sizeof(C) / 4];
-  if (units) {
-    ld_words(vp, wv, pol);
-    ld_words(cp, wc, pol);
-  }
+  constexpr int NV = S * sizeof(T) / 4, NC = S * sizeof(C) / 4;
+  // the values and columns of units u .. u+DEPTH-1 in flight while unit u is
+  // consumed
+  uint32_t wv[DEPTH][NV], wc[DEPTH][NC];
+#pragma unroll
+  for (int s = 0; s < DEPTH; s++)
+    if ((uint32_t)s < units) {
+      ld_words(vp + s * S * WS, wv[s], pol);
+      ld_words(cp + s * S * WS, wc[s], pol);
+    }
 #pragma unroll 1
   for (uint32_t u = 0; u < units; u++) {
-    uint32_t nv[S * sizeof(T) / 4], nc[S * sizeof(C) / 4], wd[S * sizeof(T) / 4];
-    if (u + 1 < units) {
-      ld_words(vp + S * WS, nv, pol);
-      ld_words(cp + S * WS, nc, pol);
+    uint32_t nv[NV], nc[NC], wd[NV];
+    if (u + DEPTH < units) {
+      ld_words(vp + DEPTH * S * WS, nv, pol);
+      ld_words(cp + DEPTH * S * WS, nc, pol);
     }
     const int step = (int)(u * S + sl);
 #pragma unroll
     for (int m = 0; m < S; m++) {
-      const P g = __ldg(xdy + word_col<C>(wc, m, base));
-      acc[m] = fma(word_val<T>(wv, m), g.y, acc[m]);
+      const P g = __ldg(xdy + word_col<C>(wc[0], m, base));
+      acc[m] = fma(word_val<T>(wv[0], m), g.y, acc[m]);
       const int q = S * (int)(lane % R) + m;
       const T dv = step < sel[q] ? sdy[q] * g.x : T(0);
       if constexpr (CSR)
@@ -244,12 +253,19 @@ __device__ __forceinline__ T adjoint_warp_slots(const int4 d, const C *__restric
       if (((u + 1) * S) % ADJ_CSR_CHUNK == 0)
         flush_csr_chunk(dvals, stg, skb, sel, (u + 1) * S - ADJ_CSR_CHUNK, ADJ_CSR_CHUNK, lane);
     } else {
-      st_words(dp, wd);
+      st_words(dp, wd, pol);
     }
 #pragma unroll
-    for (int q = 0; q < (int)(S * sizeof(T) / 4); q++) wv[q] = nv[q];
+    for (int s = 0; s + 1 < DEPTH; s++) {
 #pragma unroll
-    for (int q = 0; q < (int)(S * sizeof(C) / 4); q++) wc[q] = nc[q];
+      for (int q = 0; q < NV; q++) wv[s][q] = wv[s + 1][q];
+#pragma unroll
+      for (int q = 0; q < NC; q++) wc[s][q] = wc[s + 1][q];
+    }
+#pragma unroll
+    for (int q = 0; q < NV; q++) wv[DEPTH - 1][q] = nv[q];
+#pragma unroll
+    for (int q = 0; q < NC; q++) wc[DEPTH - 1][q] = nc[q];
     vp += S * WS;
     cp += S * WS;
     dp += S * WS;
@@ -264,7 +280,7 @@ __device__ __forceinline__ T adjoint_warp_slots(const int4 d, const C *__restric
     if constexpr (CSR)
       stg[lane][(units * S + i) % ADJ_CSR_CHUNK] = dv;
     else
-      dvals[o + k] = dv;
+      __stcs(dvals + o + k, dv);
   }
   if constexpr (CSR) {  // the last, partial chunk
     const uint32_t c0 = (units * S / ADJ_CSR_CHUNK) * ADJ_CSR_CHUNK;
@@ -273,31 +289,37 @@ __device__ __forceinline__ T adjoint_warp_slots(const int4 d, const C *__restric
   return combine_lanes<S>(acc, lane) + tail;
 }
 
-// Three resident blocks per SM (80 registers) with the next unit's loads in
-// flight, and the rows' dy / slot counts read from shared memory instead of
-// held in 16 registers per lane, measured 9 % faster than the first form (76
-// registers, two units unrolled) at hex 64^3, fp32.
-// Blocks per SM the registers are capped for: fp64 in slot order runs 4 %
-// faster with four (64 registers); the others measured best with three.
+// Launch shape per value type and dvals order: units of loads in flight per
+// lane (DEPTH), warps per block and the blocks per SM the registers are
+// capped for.  fp32: two units in flight, five blocks of 4 warps (96
+// registers), 5 % faster in slot order than one unit with three blocks of 8
+// warps (80 registers) at hex 64^3; the rows' dy / slot counts are read from
+// shared memory instead of held in 16 registers per lane.  fp64 in slot
+// order runs 4 % faster with four blocks of 8 warps (64 registers) than with
+// three; a ring of load sets unrolled over the loop (no register moves)
+// measured slower for fp32 and fp64 slot order.
 template <typename T, bool CSR>
-constexpr int adj_min_blocks() {
-  return sizeof(T) == 8 && !CSR ? 4 : 3;
-}
+struct AdjCfg {
+  static constexpr int depth = sizeof(T) == 4 ? 2 : 1;
+  static constexpr int warps = sizeof(T) == 4 ? 4 : 8;
+  static constexpr int min_blocks = sizeof(T) == 4 ? 5 : (CSR ? 3 : 4);
+};
 
 // CSR: dvals in CSR order (rowptr gives each row's first entry), staged in
 // shared memory per chunk of steps.
 template <typename T, bool COMP, bool CSR>
-__global__ void __launch_bounds__(256, (adj_min_blocks<T, CSR>())) k_adjoint_sym_slots(
+__global__ void __launch_bounds__(AdjCfg<T, CSR>::warps * 32, AdjCfg<T, CSR>::min_blocks) k_adjoint_sym_slots(
     const int4 *__restrict__ desc, uint32_t W, const int32_t *__restrict__ row_map, const uint32_t *__restrict__ slen,
     const int32_t *__restrict__ rowptr, uint32_t nzr, uint32_t nrows, const int32_t *__restrict__ pc,
     const uint16_t *__restrict__ c16, const int32_t *__restrict__ c32, const int4 *__restrict__ cdesc,
     const T *__restrict__ tv, const typename Pair<T>::type *__restrict__ xdy, T *__restrict__ dx,
     T *__restrict__ dvals) {
   using namespace core;
-  __shared__ T s_dy[8][32];
-  __shared__ int s_el[8][32];
-  __shared__ int s_kb[CSR ? 8 : 1][32];
-  __shared__ T s_stage[CSR ? 8 : 1][32][ADJ_CSR_CHUNK + 1];
+  constexpr int NW = AdjCfg<T, CSR>::warps, DEPTH = AdjCfg<T, CSR>::depth;
+  __shared__ T s_dy[NW][32];
+  __shared__ int s_el[NW][32];
+  __shared__ int s_kb[CSR ? NW : 1][32];
+  __shared__ T s_stage[CSR ? NW : 1][32][ADJ_CSR_CHUNK + 1];
   const uint32_t lane = threadIdx.x & 31;
   const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
   if (w < W) {
@@ -330,13 +352,13 @@ __global__ void __launch_bounds__(256, (adj_min_blocks<T, CSR>())) k_adjoint_sym
     if constexpr (COMP) {
       const int4 cd = cdesc[w];
       if (cd.y == 0)
-        total = adjoint_warp_slots<T, uint16_t, CSR>(d, c16 + (uint32_t)d.x, cd.x, tv, xdy, dvals, sdy, sel, skb, stg,
+        total = adjoint_warp_slots<T, uint16_t, CSR, DEPTH>(d, c16 + (uint32_t)d.x, cd.x, tv, xdy, dvals, sdy, sel, skb, stg,
                                                      dyr, el, lane, pol);
       else
-        total = adjoint_warp_slots<T, int32_t, CSR>(d, c32 + (uint32_t)cd.z, 0, tv, xdy, dvals, sdy, sel, skb, stg,
+        total = adjoint_warp_slots<T, int32_t, CSR, DEPTH>(d, c32 + (uint32_t)cd.z, 0, tv, xdy, dvals, sdy, sel, skb, stg,
                                                     dyr, el, lane, pol);
     } else {
-      total = adjoint_warp_slots<T, int32_t, CSR>(d, pc + (uint32_t)d.x, 0, tv, xdy, dvals, sdy, sel, skb, stg, dyr,
+      total = adjoint_warp_slots<T, int32_t, CSR, DEPTH>(d, pc + (uint32_t)d.x, 0, tv, xdy, dvals, sdy, sel, skb, stg, dyr,
                                                   el, lane, pol);
     }
     for (uint32_t k = 1; k < T_; k <<= 1) total += __shfl_down_sync(0xffffffffu, total, k);
@@ -516,13 +538,14 @@ extern "C" wk_status wk_adjoint_run(wk_adjoint *a, const void *x, const void *dy
     if (a->xdy.bytes < pb) WK_TRY(a->xdy.alloc(pb));
     const unsigned gi = grid_for(n, 256);
 #define WK_ADJ_SLOTS1(T, COMP, CSR)                                                                                 \
-  k_adjoint_sym_slots<T, COMP, CSR><<<gs, 256, 0, st>>>(                                                            \
+  k_adjoint_sym_slots<T, COMP, CSR><<<(unsigned)std::max<size_t>(1, ((size_t)W + AdjCfg<T, CSR>::warps - 1) /      \
+                                                          AdjCfg<T, CSR>::warps),                                  \
+                                      AdjCfg<T, CSR>::warps * 32, 0, st>>>(                                        \
       L->d.warp_desc, W, L->d.row_map, L->d.slen, L->d.rowptr, L->info.nznrows, n, f->cols.as<int32_t>(),           \
       f->c16.as<uint16_t>(), f->c32.as<int32_t>(), f->cdesc.as<int4>(), a->te->vals.as<T>(),                        \
       a->xdy.as<typename Pair<T>::type>(), (T *)dx, (T *)dvals)
 #define WK_ADJ_SLOTS(T)                                                                                             \
   do {                                                                                                              \
-    const unsigned gs = (unsigned)std::max<size_t>(1, ((size_t)W + 7) / 8);                                        \
     if (f->compressed) {                                                                                            \
       if (slots) WK_ADJ_SLOTS1(T, true, false); else WK_ADJ_SLOTS1(T, true, true);                                  \
     } else {                                                                                                        \
