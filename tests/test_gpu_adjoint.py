@@ -219,3 +219,57 @@ def test_one_sided_adjoints_match_the_full_adjoint(value_order):
         assert rel(dx1.cpu().numpy(), dx.cpu().numpy()) < 1e-14
         y_ref = O.csr_spmv_t(rp, cols, vals, dy.cpu().numpy(), n)
         assert rel(dx1.cpu().numpy(), y_ref) < 1e-12
+
+
+def _pattern_symmetric_csr(rng, n, maxlen):
+    """Random CSR whose pattern is symmetric (P ∪ Pᵀ plus the diagonal) and
+    whose values are not."""
+    rp, cols, _ = random_csr(rng, n, maxlen)
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    r = np.concatenate([rows, cols, np.arange(n)]).astype(np.int64)
+    c = np.concatenate([cols, rows, np.arange(n)]).astype(np.int64)
+    key = np.unique(r * n + c)
+    r, c = key // n, key % n
+    rp2 = np.zeros(n + 1, np.int64)
+    np.add.at(rp2, r + 1, 1)
+    return np.cumsum(rp2).astype(np.int32), c.astype(np.int32), rng.standard_normal(len(c))
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_fused_path_on_every_small_warp_count(dtype):
+    """The fused symmetric adjoint launches several layout warps per block:
+    layouts of 1-8 warps (counts that do and do not fill the last block), both
+    value orders, 32- and 16-bit columns, against the host gradient; padding
+    slots of a slot-order gradient stay 0."""
+    import torch
+
+    from warpkernel_gb300.autograd import WPKMatrix
+    dt = getattr(torch, dtype)
+    rng = np.random.default_rng(11)
+    for n in (20, 40, 70, 100, 140, 200, 230):
+        rp, cols, vals = _pattern_symmetric_csr(rng, n, min(6, n // 3))
+        rows = np.repeat(np.arange(n), np.diff(rp))
+        x, dy = rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)
+        npdt = np.float64 if dtype == "float64" else np.float32
+        vh, xh, dyh = vals.astype(npdt), x.astype(npdt), dy.astype(npdt)
+        dx_ref = O.csr_spmv_t(rp, cols, vh.astype(np.float64), dyh.astype(np.float64), n)
+        dv_ref = dyh[rows] * xh[cols]
+        xt, dyt = torch.from_numpy(xh).cuda(), torch.from_numpy(dyh).cuda()
+        for kind, th in ((1, None), (2, 4)):
+            v = torch.from_numpy(vh).cuda()
+            m_csr = WPKMatrix(rp, cols, v, kind=kind, threshold=th)
+            assert m_csr.symmetric
+            m_slot = WPKMatrix(rp, cols, m_csr.to_slots(v), kind=kind, threshold=th, value_order="slots")
+            for compress in (False, True):
+                for mat in (m_csr, m_slot):
+                    if compress:
+                        mat.eng.compress_cols()
+                    dx, dv = mat.adjoint(xt, dyt)
+                    if mat is m_slot:
+                        pad = torch.ones(mat.allocate_nz, dtype=torch.bool, device="cuda")
+                        pad[mat._reorder_rows()] = False
+                        assert not torch.any(dv[pad] != 0)
+                        dv = mat.to_csr(dv)
+                    tol = 1e-13 if dtype == "float64" else 1e-5
+                    assert rel(dx.double().cpu().numpy(), dx_ref) < tol, (n, kind, compress)
+                    assert np.array_equal(dv.cpu().numpy(), dv_ref), (n, kind, compress)
