@@ -426,6 +426,27 @@ def suite_adjoint(reps):
             tb = _event_ms(lambda: (fwd(), adj()), reps)
             out["slots+cols16"] = {"fwd_ms": round(tf, 4), "adj_ms": round(ta, 4), "fwd_plus_adj_ms": round(tb, 4),
                                    "ratio": round(tb / tf, 3)}
+    # a general (unsymmetric) pattern: the same matrix with 1 % of its
+    # off-diagonal entries dropped (seed 5), so the adjoint takes the
+    # transposed engine's SpMV for dx and a second pass for dvals
+    gen = torch.Generator(device="cuda").manual_seed(5)
+    rpc = rp.to("cuda", torch.int64)
+    rows = torch.repeat_interleave(torch.arange(n, device="cuda"), rpc[1:] - rpc[:-1])
+    cc = cols.to("cuda", torch.int64)
+    keep = (rows == cc) | (torch.rand(nnz, device="cuda", generator=gen) > 0.01)
+    rows_k = rows[keep]
+    rp_k = torch.zeros(n + 1, dtype=torch.int64, device="cuda")
+    rp_k[1:] = torch.cumsum(torch.bincount(rows_k, minlength=n), 0)
+    v_k = vals.to("cuda")[keep].float()
+    g_csr = WPKMatrix(rp_k.to(torch.int32), cc[keep].to(torch.int32), v_k, kind=2, threshold=81)
+    g_slot = WPKMatrix(rp_k.to(torch.int32), cc[keep].to(torch.int32), g_csr.to_slots(v_k), kind=2, threshold=81,
+                       value_order="slots")
+    y = torch.zeros(n, dtype=torch.float32, device="cuda")
+    tf = _event_ms(lambda: g_csr.eng.run(0, 128, x, y, timed=False), reps)
+    out["general_pattern"] = {"nnz": int(keep.sum().item()), "symmetric": g_csr.symmetric, "fwd_ms": round(tf, 4)}
+    for order, m in (("csr", g_csr), ("slots", g_slot)):
+        ta = _event_ms(lambda: m.adjoint(x, dy), reps)
+        out["general_pattern"][f"{order}_adj_ms"] = round(ta, 4)
     return out
 
 
