@@ -5,7 +5,7 @@
 //    product, then fma per step, then the tree) -- bit-identical to the oracle
 //    and to the reference kernels compiled with contraction;
 //  * fast: several slots per lane per iteration (VecPlan: 4 for fp64, 8 for
-//    fp32 and scaled FP16, 16 for bf16) with 256/128-bit loads, rows
+//    fp32, 16 for bf16 and scaled FP16) with 256/128-bit loads, rows
 //    re-associated.
 // The matrix stream is loaded with ld.global.nc.L1::no_allocate and an L2
 // evict_first policy so that x (gathered with ld.global.nc with cache != 0,

@@ -221,13 +221,15 @@ struct SlotsPerLane {
 // boxes and slower on others, so they keep the plain loop.
 template <typename V, typename C>
 struct VecPlan {
-  static constexpr int slots = std::is_same<V, __nv_bfloat16>::value ? 16 : SlotsPerLane<V>::value;
-  // units unrolled in the plain loop: scaled FP16 with 16-bit columns (4 B
-  // per slot, FP32 x) runs 7 % faster with 4 on two boxes; fp64 runs 1.3 %
-  // faster with 1 (2 and 3 unrolled units cost registers and 1-6 %) except on
-  // layouts of long warps, where k_spmv_fast overrides it with 2; bf16 with
-  // 16-bit columns lost 2 % with 4, so the others keep 2
-  static constexpr int unroll = (std::is_same<V, __half>::value && sizeof(C) == 2) ? 4 : sizeof(V) == 8 ? 1 : 2;
+  static constexpr int slots =
+      (std::is_same<V, __nv_bfloat16>::value || std::is_same<V, __half>::value) ? 16 : SlotsPerLane<V>::value;
+  // units unrolled in the plain loop: fp64 runs 1.3 % faster with 1 (2 and 3
+  // unrolled units cost registers and 1-6 %) except on layouts of long warps,
+  // where k_spmv_fast overrides it with 2; bf16 with 16-bit columns lost 2 %
+  // with 4, so the others keep 2.  Scaled FP16 takes 16 slots per lane like
+  // bf16 (32-byte value loads): with 16-bit columns 3.6 % faster than 8 slots
+  // with 4 units unrolled, 0.5 % slower with 32-bit columns.
+  static constexpr int unroll = sizeof(V) == 8 ? 1 : 2;
   static constexpr bool pipelined = sizeof(V) == 4 && sizeof(C) == 4;
 };
 // The CG's SpMV-dot (FP32 p for every narrow value type, plus the dot
@@ -363,7 +365,8 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict_
   // pipe).  With 4 slots per lane (fp64) their operands are loaded before the
   // combine, whose shuffles then overlap the loads: loading them after it
   // made layouts of long warps 15 % slower; with 8 slots the 14 preloaded
-  // registers made scaled FP16 with 16-bit columns 10 % slower.
+  // registers made scaled FP16 with 16-bit columns (then on 8 slots) 10 %
+  // slower.
   const size_t ut = (size_t)units * S * WS + lane;
   if constexpr (S <= 4) {
     Acc tv[S - 1], tx[S - 1];
@@ -390,7 +393,7 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict_
     }
     return s;
   } else {
-    // 16 slots per lane (bf16): the tail can be up to 15 steps, so it is summed
+    // 16 slots per lane (bf16, scaled FP16): the tail can be up to 15 steps, so it is summed
     // before the combine (its loads overlap the combine's shuffles) and added
     // after it -- an FP32 add, not one on the FP64 pipe; 5-9 % faster on
     // layouts of 27-41 steps (with 8 slots the fold measured faster for fp32)
