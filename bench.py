@@ -264,6 +264,20 @@ def run_ours(args):
                      "kernel_ms_median": round(statistics.median(kern_times), 5),
                      "alg_bytes_per_launch": B},
     }
+    if rank == 0 and not args.no_parity:
+        # every device-built layout array, the padded arrays, the renumbered
+        # columns and x, and the exact-order run against the oracle's host
+        # restatement on this matrix (after the timed region)
+        from oracle import parity
+        y_ex = torch.zeros(n, dtype=torch.float64, device="cuda")
+        eng.run(nb, bs, x, y_ex, cache=True, order=1, stream=stream, timed=False)
+        torch.cuda.synchronize()
+        par = parity.compare(k, eng, rp_h, cols_h, vals_h, x_h, args.kind, args.threshold if args.kind == 2 else 0,
+                             y_exact=y_ex.cpu().numpy(), y_fast=y_host, cols_dev=cols, x_dev=x)
+        out["parity_c2" if args.mesh == 128 else f"parity_hex{args.mesh}"] = {
+            "against": "oracle restatement of the reference's host scan / process / reorderings / run (fma)",
+            **par}
+        del y_ex
     if rank == 0 and not args.no_cpu_baseline:
         med, nth, reps, y_cpu = cpu_csr_baseline(rp_h, cols_h, vals_h, x_h, budget_s=args.cpu_budget)
         out["cpu_baseline"] = {"value": round(B / med / 1e9, 2), "unit": "GB/s", "cores": nth, "kind": "port",
@@ -346,12 +360,18 @@ def suite_mixed_and_cg(reps):
     cg = wk.wpk.cg(e64, b, xc, tol=1e-10, max_iter=20000, check_every=16)
     xi = torch.zeros_like(b)
     ir = wk.wpk.ir_cg(e64, engines["f32"], b, xi, tol=1e-10, inner_tol=1e-5, max_inner=20000, check_every=16)
+    xi32 = torch.zeros_like(b)
+    ir32 = wk.wpk.ir_cg(e64, engines["f32"], b, xi32, tol=1e-10, inner_tol=1e-5, max_inner=20000, check_every=16,
+                        inner_dots="fp32")
     xb = torch.zeros_like(b)
     irb = wk.wpk.ir_cg(e64, engines["bf16"], b, xb, tol=1e-10, inner_tol=1e-2, max_inner=20000, check_every=16)
     xh = torch.zeros_like(b)
     irh = wk.wpk.ir_cg(e64, engines["f16s"], b, xh, tol=1e-10, inner_tol=1e-3, max_inner=20000, check_every=16)
-    res["cg"] = {"fp64_cg": cg, "ir_cg_f32_inner": ir, "ir_cg_bf16_inner": irb, "ir_cg_f16s_inner": irh,
+    res["cg"] = {"inner_dot_products": "fp64 unless named fp32_dots",
+                 "fp64_cg": cg, "ir_cg_f32_inner_fp64_dots": ir, "ir_cg_f32_inner_fp32_dots": ir32,
+                 "ir_cg_bf16_inner": irb, "ir_cg_f16s_inner": irh,
                  "ir_f32_speedup": round(cg["seconds"] / ir["seconds"], 3),
+                 "ir_f32_fp32_dots_speedup": round(cg["seconds"] / ir32["seconds"], 3),
                  "ir_bf16_speedup": round(cg["seconds"] / irb["seconds"], 3),
                  "ir_f16s_speedup": round(cg["seconds"] / irh["seconds"], 3)}
     return res
@@ -828,6 +848,8 @@ def main():
     ap.add_argument("--mesh", type=int, default=128, help="hex elements per axis (128 = the headline)")
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the full-size comparison of the layout and run with the oracle")
     ap.add_argument("--no-suites", action="store_true",
                     help="skip the mixed-precision / CG / adjoint / batched measurements")
     ap.add_argument("--value-dtype", choices=["f16s", "f32", "bf16"], default="f16s",

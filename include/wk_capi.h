@@ -322,8 +322,12 @@ wk_status wk_residual(wk_engine *e, const double *x, const double *b, double *r,
  * partial sums go to a static device array of 65,536 doubles (512 KiB) that
  * every GPU loading the library keeps until the process exits.  Layouts with
  * more than 262,144 warps are rejected with WK_ERR_INVALID.  The first call on
- * a device looks up that array's address (cudaGetSymbolAddress), so make it
- * once per device before any stream capture.  All calls share the array:
+ * each engine looks up that array's address (cudaGetSymbolAddress) and keeps
+ * it in the engine.  Under CUDA's lazy module loading (the default), the first
+ * call on a device also loads the code that holds the array, which reserves
+ * its 512 KiB at that moment -- itself a device allocation.  So make one call
+ * per engine during set-up, before any stream capture and before the phase in
+ * which nothing may allocate.  All calls share the array:
  * calls whose kernels overlap on the GPU (other streams, other threads) race
  * and must be serialised by the caller.  Creating the engine allocates; this
  * call does not. */
@@ -352,6 +356,10 @@ typedef struct {
   int outer;
   double relres;
   double seconds;
+  /* wk_ir_cg: 0 (default) sums the inner solve's dot products p.q and r.r in
+   * FP64 (each FP32 element converted once); 1 sums each thread's and each
+   * block's share in FP32 and only the block partials in FP64. */
+  int inner_dots_fp32;
 } wk_cg_params;
 
 /* fp64 CG on an fp64 engine; b, x (initial guess, overwritten) are device
@@ -363,8 +371,8 @@ wk_status wk_cg(wk_engine *e, const double *b, double *x, wk_cg_params *p, void 
  * correction d solves A d = r with an fp32 CG on the low-precision engine `lo`
  * (WK_F32, WK_BF16 or WK_F16S values, compressed columns if
  * wk_engine_compress_cols was called): fp32 vectors updated in fp32
- * arithmetic, dot products summed in fp32 within a block and in fp64 across
- * blocks. */
+ * arithmetic, the inner dot products summed in fp64 (or, with
+ * p->inner_dots_fp32 = 1, in fp32 within a block and fp64 across blocks). */
 wk_status wk_ir_cg(wk_engine *e64, wk_engine *lo, const double *b, double *x, wk_cg_params *p,
                    void *stream);
 

@@ -512,6 +512,87 @@ void wko_run_f64_omp(const wko_layout *l, const double *pvals, const int32_t *pc
   }
 }
 
+/* ---- reduced-precision storage ------------------------------------------ */
+
+void wko_round_f32(const double *in, float *out, int64_t n) {
+  for (int64_t i = 0; i < n; i++) out[i] = (float)in[i]; /* C conversion: nearest-even */
+}
+
+/* fp64 -> bf16 (8 significant bits, float's exponent range), rounded to
+ * nearest-even in one step: the quantum of |d| is 2^(e-8) for d = m 2^e,
+ * m in [0.5, 1), but never below bf16's subnormal step 2^-133; rint() rounds
+ * the scaled value to an integer (ties to even in the default rounding mode),
+ * which scaling back leaves exact.  Results of 2^128 and above overflow to inf. */
+static uint16_t bf16_rne(double d) {
+  const uint16_t sign = signbit(d) ? 0x8000u : 0u;
+  if (isnan(d)) return 0x7fffu;
+  if (isinf(d)) return sign | 0x7f80u;
+  const double a = fabs(d);
+  if (a == 0.0) return sign;
+  int e;
+  (void)frexp(a, &e);
+  int qe = e - 8;
+  if (qe < -133) qe = -133;
+  const double r = ldexp(rint(ldexp(a, -qe)), qe);
+  if (r >= 0x1p128) return sign | 0x7f80u;
+  const float f = (float)r; /* exact: r has at most 8 significant bits */
+  uint32_t u;
+  memcpy(&u, &f, 4);
+  return (uint16_t)(sign | (u >> 16));
+}
+
+void wko_round_bf16(const double *in, uint16_t *out, int64_t n) {
+  for (int64_t i = 0; i < n; i++) out[i] = bf16_rne(in[i]);
+}
+
+static inline float lp_at(int vtype, const void *v, size_t i) {
+  if (vtype == 0) return ((const float *)v)[i];
+  uint32_t u = (uint32_t)((const uint16_t *)v)[i] << 16;
+  float f;
+  memcpy(&f, &u, 4);
+  return f;
+}
+
+/* lane_sum in FP32: first product (a float multiply), then fmaf per step. */
+static float lane_sum_lp(int vt, const void *A, const int32_t *c, const void *x, int32_t toffset,
+                         uint32_t maxrows) {
+  uint32_t maxnz = maxrows * WS + (uint32_t)toffset;
+  float sum = lp_at(vt, A, (size_t)toffset) * lp_at(vt, x, (size_t)c[toffset]);
+  for (toffset += (int32_t)WS; (uint32_t)toffset < maxnz; toffset += (int32_t)WS)
+    sum = fmaf(lp_at(vt, A, (size_t)toffset), lp_at(vt, x, (size_t)c[toffset]), sum);
+  return sum;
+}
+
+void wko_run_lp(const wko_layout *l, int vt, const void *pvals, const int32_t *pcols, const void *x,
+                float *y, int mapped, int nthreads) {
+  if (nthreads <= 0) nthreads = wko_max_threads();
+  long W = (long)l->nwarps;
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+  for (long wl = 0; wl < W; wl++) {
+    const uint32_t w = (uint32_t)wl;
+    const uint32_t T = l->kind == 2 ? l->threads_per_row[w] : 1u;
+    const uint32_t row_start = l->kind == 2 ? l->row_offset_warp[w] : w * WS;
+    float s[32];
+    for (uint32_t lane = 0; lane < WS; lane++) {
+      s[lane] = 0.0f;
+      if (row_start + lane / T < l->nznrows)
+        s[lane] = lane_sum_lp(vt, pvals, pcols, x, l->warp_offsets[w] + (int32_t)lane, l->max_nz_rows[w]);
+    }
+    for (uint32_t lead = 0; lead < WS; lead += T) {
+      const uint32_t rowid = row_start + lead / T;
+      if (rowid >= l->nznrows) continue;
+      float t[32];
+      for (uint32_t k = 0; k < T; k++) t[k] = s[lead + k];
+      for (uint32_t i = 1; i < T; i <<= 1)
+        for (uint32_t k = 0; k + i < T; k += 2 * i) t[k] = t[k] + t[k + i];
+      if (mapped)
+        y[l->row_map[rowid]] = t[0];
+      else
+        y[rowid] = t[0];
+    }
+  }
+}
+
 void wko_csr_spmv_f64(const int32_t *rowptr, const int32_t *cols, const double *vals,
                       const double *x, double *y, uint32_t nrows, int nthreads) {
   if (nthreads <= 0) nthreads = wko_max_threads();

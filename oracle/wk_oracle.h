@@ -85,6 +85,21 @@ void wko_run_f64(const wko_layout *l, const double *pvals, const int32_t *pcols,
 void wko_run_x_f64(const wko_layout *l, const double *pvals, const int32_t *pcols,
                    const double *x, double *y, int fma_mode);
 
+/* Reduced-precision storage (no reference counterpart): the library rounds
+ * fp64 values and x to FP32 or BF16 once, round-to-nearest-even, and sums in
+ * FP32.  wko_round_f32 / wko_round_bf16 round each fp64 input in one step
+ * (bf16 as raw bits).  wko_run_lp is the documented order of
+ * warpkernel.hpp:65-71 / 147-162 in FP32: per lane the first product, then
+ * fmaf per step of 32 slots, then the WPK2 pairwise tree; vtype 0 = FP32
+ * values and x, 1 = BF16 values and x (raw bits); y is FP32; mapped 1 = run
+ * (y[row_map[p]]), 0 = run_x (y[p]).  Rows without entries are not written.
+ * OpenMP across layout warps (nthreads <= 0: all threads); the per-row
+ * arithmetic does not depend on the thread count. */
+void wko_round_f32(const double *in, float *out, int64_t n);
+void wko_round_bf16(const double *in, uint16_t *out, int64_t n);
+void wko_run_lp(const wko_layout *l, int vtype, const void *pvals, const int32_t *pcols, const void *x,
+                float *y, int mapped, int nthreads);
+
 /* Plain CSR multiply y = A x (row-parallel, OpenMP, static schedule); the
  * multicore CPU baseline.  nthreads <= 0 uses all available threads. */
 void wko_csr_spmv_f64(const int32_t *rowptr, const int32_t *cols, const double *vals,

@@ -23,6 +23,7 @@ _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 _u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_u16p = np.ctypeslib.ndpointer(np.uint16, flags="C_CONTIGUOUS")
 
 
 class _Layout(C.Structure):
@@ -70,6 +71,9 @@ def lib():
         L.wko_verify.argtypes = [C.c_uint32, _f64p, _f64p, C.POINTER(C.c_long)]
         L.wko_verify_x.argtypes = [lp, _f64p, _f64p, C.POINTER(C.c_long)]
         L.wko_max_threads.restype = C.c_int
+        L.wko_round_f32.argtypes = [_f64p, _f32p, C.c_int64]
+        L.wko_round_bf16.argtypes = [_f64p, _u16p, C.c_int64]
+        L.wko_run_lp.argtypes = [lp, C.c_int, C.c_void_p, _i32p, C.c_void_p, _f32p, C.c_int, C.c_int]
         L.wko_fe_size.argtypes = [C.c_int] * 5 + [C.POINTER(C.c_int64)] * 2
         L.wko_fe_fill.argtypes = [C.c_int] * 6 + [C.c_uint64, C.c_void_p, C.c_void_p,
                                                   C.c_void_p, C.c_int]
@@ -227,6 +231,29 @@ class OracleLayout:
                             np.ascontiguousarray(x, np.float64), y, int(fma))
         return y
 
+    def run_lp(self, pvals, pcols, x, mapped=True, y=None, nthreads=0):
+        """Documented order in FP32 (wko_run_lp): pvals / x float32 (FP32
+        storage) or uint16 bf16 bits (BF16 storage); returns float32 y."""
+        pvals = np.ascontiguousarray(pvals)
+        x = np.ascontiguousarray(x)
+        if pvals.dtype == np.float32 and x.dtype == np.float32:
+            vt = 0
+        elif pvals.dtype == np.uint16 and x.dtype == np.uint16:
+            vt = 1
+        else:
+            raise TypeError("pvals and x must both be float32 or both uint16 (bf16 bits)")
+        y = np.zeros(self.layout.nrows, np.float32) if y is None else y
+        lib().wko_run_lp(C.byref(self.c), vt, pvals.ctypes.data, np.ascontiguousarray(pcols, np.int32),
+                         x.ctypes.data, y, int(mapped), int(nthreads))
+        return y
+
+    def place(self, vals):
+        """structure::reorder for any element type: vals (CSR order) placed at
+        reorder_rows, padding slots 0 (warpkernel.hpp:385-394)."""
+        out = np.zeros(self.layout.allocate_nz, np.asarray(vals).dtype)
+        out[self.layout.reorder_rows] = vals
+        return out
+
     def run_omp(self, pvals, pcols, x, y, nthreads=0):
         lib().wko_run_f64_omp(C.byref(self.c), pvals, pcols, x, y, int(nthreads))
         return y
@@ -260,6 +287,27 @@ def csr_spmv_t(rowptr, cols, vals, x, ncols):
                              np.ascontiguousarray(vals, np.float64),
                              np.ascontiguousarray(x, np.float64), y, len(rowptr) - 1, ncols)
     return y
+
+
+def round_f32(x):
+    """fp64 -> FP32, round-to-nearest-even (the library's conversion)."""
+    x = np.ascontiguousarray(x, np.float64)
+    out = np.zeros(len(x), np.float32)
+    lib().wko_round_f32(x, out, len(x))
+    return out
+
+
+def round_bf16(x):
+    """fp64 -> BF16 bits (uint16), round-to-nearest-even in one step."""
+    x = np.ascontiguousarray(x, np.float64)
+    out = np.zeros(len(x), np.uint16)
+    lib().wko_round_bf16(x, out, len(x))
+    return out
+
+
+def bf16_to_f32(b):
+    """BF16 bits (uint16) -> float32 (exact)."""
+    return (np.ascontiguousarray(b, np.uint16).astype(np.uint32) << 16).view(np.float32)
 
 
 def max_threads():

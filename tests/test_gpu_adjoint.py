@@ -273,3 +273,74 @@ def test_fused_path_on_every_small_warp_count(dtype):
                     tol = 1e-13 if dtype == "float64" else 1e-5
                     assert rel(dx.double().cpu().numpy(), dx_ref) < tol, (n, kind, compress)
                     assert np.array_equal(dv.cpu().numpy(), dv_ref), (n, kind, compress)
+
+
+@pytest.mark.parametrize("value_order", ["csr", "slots"])
+def test_gradient_at_benchmark_size_hex64(value_order):
+    """The differentiable-SpMV workload at full size: hex 64^3, 3 dof
+    (823,875 rows, 64,701,513 nnz, seed 4), fp64, loss = 0.5 ||A(vals) x -
+    t||^2 through torch.autograd: the whole gradient against the host
+    CSR-transpose gradient, and 64 value entries and 64 x entries against
+    central finite differences.  Each perturbed loss is evaluated on the host
+    from scratch for the rows the entry touches (one row for a value, the
+    rows of column i for x[i]); the rows it does not touch contribute the
+    same terms to both evaluations and cancel exactly."""
+    import torch
+
+    from warpkernel_gb300 import fe
+    from warpkernel_gb300.autograd import WPKMatrix
+    rp_d, cols_d, vals_d = fe.fe_matrix(3, 64, 64, 64, 3, 1, 4)
+    rp, cols, vals = rp_d.cpu().numpy(), cols_d.cpu().numpy(), vals_d.cpu().numpy()
+    n = len(rp) - 1
+    assert (n, len(cols)) == (823_875, 64_701_513)
+    x = fe.uniform_vec(4, 0, n).cpu().numpy()
+    t = fe.uniform_vec(4, 1, n).cpu().numpy()
+    mat = WPKMatrix(rp_d, cols_d, vals_d, kind=2, threshold=81)
+    if value_order == "slots":
+        mat = WPKMatrix(rp_d, cols_d, mat.to_slots(vals_d), kind=2, threshold=81, value_order="slots")
+    assert mat.symmetric
+    v = (vals_d if value_order == "csr" else mat.to_slots(vals_d)).clone().requires_grad_(True)
+    xx = torch.from_numpy(x).cuda().requires_grad_(True)
+    y = mat.matvec(v, xx)
+    (0.5 * torch.sum((y - torch.from_numpy(t).cuda()) ** 2)).backward()
+    dv = v.grad if value_order == "csr" else mat.to_csr(v.grad)
+    dv, dx = dv.cpu().numpy(), xx.grad.cpu().numpy()
+    y_ref, dx_ref, dv_ref = host_grads(rp, cols, vals, x, t)
+    assert rel(y.detach().cpu().numpy(), y_ref) < 1e-12
+    assert rel(dx, dx_ref) < 1e-12
+    assert rel(dv, dv_ref) < 1e-14
+
+    rows = np.repeat(np.arange(n, dtype=np.int64), np.diff(rp))
+    csc = np.argsort(cols, kind="stable")  # entries of column i: csc[cp[i]:cp[i+1]]
+    cp = np.zeros(n + 1, np.int64)
+    cp[1:] = np.cumsum(np.bincount(cols, minlength=n))
+
+    def row_loss(r, vv, xv):
+        s = 0.0
+        for k in range(rp[r], rp[r + 1]):
+            s = s + vv[k - rp[r]] * xv(cols[k])
+        return 0.5 * (s - t[r]) ** 2
+
+    rng = np.random.default_rng(64)
+    h = 1e-3
+    for k in rng.choice(len(vals), 64, replace=False):
+        r = int(rows[k])
+        seg = vals[rp[r]:rp[r + 1]].copy()
+        j = k - rp[r]
+        lp = lm = None
+        for sign in (1, -1):
+            s2 = seg.copy()
+            s2[j] += sign * h
+            val = row_loss(r, s2, lambda c: x[c])
+            lp, lm = (val, lm) if sign == 1 else (lp, val)
+        fd = (lp - lm) / (2 * h)
+        assert abs(fd - dv[k]) <= 1e-7 * max(abs(fd), 1e-3), (k, fd, dv[k])
+    for i in rng.choice(n, 64, replace=False):
+        touched = np.unique(rows[csc[cp[i]:cp[i + 1]]])
+        tot = {}
+        for sign in (1, -1):
+            xi = x[i] + sign * h
+            tot[sign] = sum(row_loss(int(r), vals[rp[r]:rp[r + 1]], lambda c: xi if c == i else x[c])
+                            for r in touched)
+        fd = (tot[1] - tot[-1]) / (2 * h)
+        assert abs(fd - dx[i]) <= 1e-7 * max(abs(fd), 1e-3), (i, fd, dx[i])

@@ -101,11 +101,13 @@ def test_ir_cg_reaches_fp64_tolerance_with_fp32_and_bf16_inner():
         lo = wk.engine(k, wk.fe.convert(torch.from_numpy(vals).cuda(), tdt), torch.from_numpy(cols).cuda(),
                        dtype=dtype)
         lo.compress_cols()
-        x = torch.zeros(n, dtype=torch.float64, device="cuda")
-        res = wk.wpk.ir_cg(e64, lo, db, x, tol=1e-10, inner_tol=1e-3 if dtype == "bf16" else 1e-4)
-        assert res["converged"] and res["relres"] <= 1e-10 and res["outer"] >= 2, (dtype, res)
-        xh = x.cpu().numpy()
-        assert np.linalg.norm(b - A @ xh) / np.linalg.norm(b) <= 1.1e-10
+        for dots in ("fp64", "fp32"):  # the inner solve's dot products
+            x = torch.zeros(n, dtype=torch.float64, device="cuda")
+            res = wk.wpk.ir_cg(e64, lo, db, x, tol=1e-10, inner_tol=1e-3 if dtype == "bf16" else 1e-4,
+                               inner_dots=dots)
+            assert res["converged"] and res["relres"] <= 1e-10 and res["outer"] >= 2, (dtype, dots, res)
+            xh = x.cpu().numpy()
+            assert np.linalg.norm(b - A @ xh) / np.linalg.norm(b) <= 1.1e-10
 
 
 def test_cg_reports_non_convergence():

@@ -167,27 +167,6 @@ def test_launch_shape_checks():
     eng.run(nb, 128, dx, dy)  # the drivers' exact grid is accepted
 
 
-def test_mixed_precision_error_bounds():
-    rp, cols, vals = O.fe_matrix(3, 12, 12, 12, 3, value_mode=1, seed=2)
-    n = len(rp) - 1
-    x = O.uniform_vec(2, 0, n)
-    y64 = O.csr_spmv(rp, cols, vals, x)
-    t = torch()
-    for dtype, tol in (("f32", 1e-6), ("bf16", 1e-2)):
-        for kind, th in ((1, 0), (2, 27)):
-            k = wk().structure() if kind == 1 else wk().structure2()
-            k.scan(len(cols), n, None, rp, None, *(() if kind == 1 else (th,)))
-            tv = t.from_numpy(vals).cuda()
-            tdt = t.float32 if dtype == "f32" else t.bfloat16
-            eng = wk().engine(k, wk().fe.convert(tv, tdt), t.from_numpy(cols).cuda(), dtype=dtype)
-            dx = wk().fe.convert(t.from_numpy(x).cuda(), tdt)
-            dy = t.zeros(n, dtype=t.float32, device="cuda")
-            for order in (0, 1):
-                eng.run(0, 256, dx, dy, order=order)
-                err = relerr(dy.double().cpu().numpy(), y64)
-                assert err < tol, (dtype, kind, order, err)
-
-
 def test_device_generator_matches_cpu_generator():
     t = torch()
     for args, mode in (((2, 20, 17, 0, 1), 0), ((3, 5, 4, 3, 3), 1), ((2, 6, 6, 0, 2), 1), ((3, 2, 2, 2, 1), 0)):
@@ -226,7 +205,8 @@ def test_compressed_columns_bit_identical_to_uncompressed():
                 assert t.equal(y0, y1), (dtype, kind, wide)
                 y2 = t.zeros(n, dtype=ydt, device="cuda")
                 eng.run_x(0, 128, dx, y2, order=0)  # run_x path of the compressed kernel
-                assert bool(t.isfinite(y2).all())
+                rm = t.from_numpy(k.row_map[:k.nznrows].astype(np.int64)).cuda()
+                assert t.equal(y2[:k.nznrows], y1[rm]), (dtype, kind)  # y'[p] = y[row_map[p]]
                 # set_colinds rebuilds the compact storage
                 eng.device_colinds = eng.device_colinds
                 y3 = t.zeros(n, dtype=ydt, device="cuda")

@@ -171,3 +171,102 @@ def test_csr_baselines_agree():
         np.add.at(A[r], cols[rp[r]:rp[r + 1]], vals[rp[r]:rp[r + 1]])
     np.testing.assert_allclose(y, A @ x, rtol=1e-12, atol=1e-12)
     np.testing.assert_allclose(O.csr_spmv_t(rp, cols, vals, x, 500), A.T @ x, rtol=1e-12, atol=1e-12)
+
+
+# ---- reduced-precision storage: the oracle's FP32 restatement --------------
+
+def _round_to(q, sig, emin):
+    """Fraction q rounded to `sig` significant bits, nearest-even, with the
+    smallest quantum 2^emin (the subnormal step); inf at 2^128 and above."""
+    from fractions import Fraction as F
+    if q == 0:
+        return 0.0
+    a = abs(q)
+    e = a.numerator.bit_length() - a.denominator.bit_length()
+    while F(2) ** e > a:
+        e -= 1
+    while F(2) ** (e + 1) <= a:
+        e += 1
+    qe = max(e - (sig - 1), emin)
+    m = a / F(2) ** qe
+    fl = m.numerator // m.denominator
+    rem = m - fl
+    if rem > F(1, 2) or (rem == F(1, 2) and fl % 2 == 1):
+        fl += 1
+    r = F(fl) * F(2) ** qe
+    v = float("inf") if r >= F(2) ** 128 else float(r)
+    return v if q > 0 else -v
+
+
+def f32(q):
+    return _round_to(q, 24, -149)
+
+
+def test_bf16_rounding_is_one_step_nearest_even():
+    """wko_round_bf16 against exact rational rounding to 8 significant bits
+    (values whose rounding through FP32 would differ included)."""
+    from fractions import Fraction as F
+    rng = np.random.default_rng(8)
+    a = rng.standard_normal(3000) * 10.0 ** rng.integers(-44, 38, 3000)
+    # ties and near-ties of the bf16 grid, reached only by exact rounding
+    a = np.concatenate([a, [1 + 2.0 ** -8, 1 + 2.0 ** -8 + 2.0 ** -40, 1 + 3 * 2.0 ** -8, 2.0 ** -134,
+                            2.0 ** -134 * (1 + 2.0 ** -30), 3.3e38, -0.0]])
+    got = O.bf16_to_f32(O.round_bf16(a)).astype(np.float64)
+    for v, g in zip(a, got):
+        want = _round_to(F(float(v)), 8, -133)
+        assert g == want or (want == 0 and g == 0), (v, g, want)
+    assert np.array_equal(O.round_f32(a), a.astype(np.float32))
+
+
+def _lp_reference(o, pv, pc, x):
+    """Per-lane first product then fused multiply-adds, then the WPK2 pairwise
+    tree, every operation rounded to FP32 exactly (Fractions)."""
+    from fractions import Fraction as F
+    L = o.layout
+    y = np.zeros(L.nrows, np.float32)
+    for w in range(L.nwarps):
+        T = int(L.threads_per_row[w]) if L.kind == 2 else 1
+        first = int(L.row_offset_warp[w]) if L.kind == 2 else 32 * w
+        s = [0.0] * 32
+        for lane in range(32):
+            if first + lane // T >= L.nznrows:
+                continue
+            off = int(L.warp_offsets[w]) + lane
+            acc = f32(F(float(pv[off])) * F(float(x[pc[off]])))
+            for i in range(1, int(L.max_nz_rows[w])):
+                k = off + 32 * i
+                acc = f32(F(float(pv[k])) * F(float(x[pc[k]])) + F(acc))
+            s[lane] = acc
+        for lead in range(0, 32, T):
+            r = first + lead // T
+            if r >= L.nznrows:
+                continue
+            t = s[lead:lead + T]
+            i = 1
+            while i < T:
+                for k in range(0, T - i, 2 * i):
+                    t[k] = f32(F(t[k]) + F(t[k + i]))
+                i *= 2
+            y[L.row_map[r]] = t[0]
+    return y
+
+
+def test_fp32_documented_order_against_exact_rounding():
+    """wko_run_lp (FP32 and BF16 storage) against the same order evaluated
+    with exact rational arithmetic and one FP32 rounding per operation, on a
+    ragged matrix with empty rows, WPK1 and WPK2 (split rows)."""
+    rng = np.random.default_rng(9)
+    rp, cols, vals = random_csr(rng, 150, 70, p_empty=0.2)
+    x = rng.uniform(-1, 1, len(rp) - 1)
+    for kind, th in ((1, 0), (2, 3), (2, 40)):
+        with O.OracleLayout(rp, kind=kind, threshold=th) as o:
+            _, pc = o.process(vals, cols)
+            for sv, sx in ((O.round_f32(vals), O.round_f32(x)), (O.round_bf16(vals), O.round_bf16(x))):
+                pv = o.place(sv)
+                y = o.run_lp(pv, pc, sx)
+                fv = pv if pv.dtype == np.float32 else O.bf16_to_f32(pv)
+                fx = sx if sx.dtype == np.float32 else O.bf16_to_f32(sx)
+                ref = _lp_reference(o, fv, pc, fx)
+                assert np.array_equal(y.view(np.uint32), ref.view(np.uint32)), (kind, th, pv.dtype)
+                y1 = o.run_lp(pv, pc, sx, nthreads=1)
+                assert np.array_equal(y1.view(np.uint32), y.view(np.uint32))

@@ -44,6 +44,22 @@ def test_residual_static_matches_allocating_entry_point():
         assert np.linalg.norm(rs - rr) / np.linalg.norm(rr) <= REL_TOL, call
         assert abs(nrm.item() - n_ref.item()) <= REL_TOL * n_ref.item(), call
         assert np.array_equal(rs, rr) and nrm.item() == n_ref.item(), call  # same kernel, same order
+    # after the set-up call, a call allocates nothing: with the library's next
+    # device allocation armed to fail it still succeeds, and the device's free
+    # memory is unchanged across it
+    x = torch.from_numpy(rng.uniform(-1, 1, n)).cuda()
+    r = torch.empty(n, dtype=torch.float64, device="cuda")
+    nrm = torch.empty(1, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    L.wk_debug_fail_alloc(1)
+    try:
+        st = L.wk_residual_static(eng.handle, x.data_ptr(), b.data_ptr(), r.data_ptr(), nrm.data_ptr(), stream)
+    finally:
+        L.wk_debug_fail_alloc(0)
+    assert st == 0
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
 
 
 def test_residual_static_rejects_layouts_beyond_its_scratch():

@@ -42,7 +42,8 @@ class LayoutInfo(C.Structure):
 class CGParams(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("max_inner", C.c_int),
                 ("inner_tol", C.c_double), ("check_every", C.c_int), ("iters", C.c_int),
-                ("outer", C.c_int), ("relres", C.c_double), ("seconds", C.c_double)]
+                ("outer", C.c_int), ("relres", C.c_double), ("seconds", C.c_double),
+                ("inner_dots_fp32", C.c_int)]
 
 
 SIGNATURES = {

@@ -1,5 +1,6 @@
 // wk_cg.cu -- conjugate gradient (fp64) and iterative-refinement CG (fp64
-// outer loop, fp32 inner CG on an FP32 / BF16 engine) on the WPK layout.
+// outer loop, fp32 inner CG on an FP32 / BF16 / scaled-FP16 engine, its dot
+// products summed in FP64 unless the caller asks for FP32) on the WPK layout.
 //
 // All scalars stay on the device.  Each reduction writes block partials that
 // a one-block kernel sums in a fixed order into a slot of `scal`, so results
@@ -56,8 +57,9 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
 
 // q = A p (rows without entries get 0) and block partials of p . q.  MODE 0:
 // vector path, 1: vector path on 16-bit columns, 2: one slot per step (short
-// warps, as wk_run's fast order chooses).
-template <typename V, typename X, int MODE>
+// warps, as wk_run's fast order chooses).  D64: p . q accumulated in FP64
+// (each row's p and q converted once), else in the vectors' precision.
+template <typename V, typename X, int MODE, bool D64>
 __global__ void __launch_bounds__(CG_BLOCK) k_spmv_dot(const V *__restrict__ pv, const int32_t *__restrict__ pc,
                                                        const uint16_t *__restrict__ c16, const int32_t *__restrict__ c32,
                                                        const int4 *__restrict__ cdesc, const int4 *__restrict__ desc,
@@ -68,9 +70,9 @@ __global__ void __launch_bounds__(CG_BLOCK) k_spmv_dot(const V *__restrict__ pv,
   if (done(scal)) return;
   __shared__ double sh[CG_BLOCK];
   const uint32_t lane = threadIdx.x & 31;
-  // p . q in the vectors' precision: FP64, or FP32 for the inner solve
-  // (no float <-> double conversions per row on GB300's FP64 pipe)
-  typedef typename std::conditional<sizeof(X) == 8, double, float>::type D;
+  // p . q in FP64 (fp64 vectors, or D64), else in FP32 for the inner solve
+  // (then no float <-> double conversions per row on GB300's FP64 pipe)
+  typedef typename std::conditional<sizeof(X) == 8 || D64, double, float>::type D;
   D part = D(0);
   const uint64_t pol = policy_evict_first();
   const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
@@ -126,10 +128,11 @@ __global__ void __launch_bounds__(1024) k_finish(const double *__restrict__ part
 
 // x += alpha p, r -= alpha q, partials of r . r; alpha = scal[rho] / scal[pq].
 // FP32 vectors (the inner solve of IR-CG, whose tolerance is loose) are
-// updated in FP32 arithmetic with each thread's r . r accumulated in FP32:
-// on GB300 the float <-> double conversions of an FP64 update run at the
-// FP64 rate and made these vector kernels FP64-bound.
-template <typename T>
+// updated in FP32 arithmetic: on GB300 the float <-> double conversions of an
+// FP64 update run at the FP64 rate and made these vector kernels FP64-bound.
+// Each thread's share of r . r is summed in FP64 with D64 (one conversion per
+// element), else in FP32.
+template <typename T, bool D64>
 __global__ void __launch_bounds__(VEC_BLOCK) k_update(T *__restrict__ x, T *__restrict__ r, const T *__restrict__ p,
                                                       const T *__restrict__ q, uint32_t n, const double *__restrict__ scal,
                                                       int i_rho, double *__restrict__ partials) {
@@ -151,9 +154,14 @@ __global__ void __launch_bounds__(VEC_BLOCK) k_update(T *__restrict__ x, T *__re
       const float ri = r[i] - a * q[i];
       x[i] = x[i] + a * p[i];
       r[i] = ri;
-      part32 = fmaf(ri, ri, part32);
+      if constexpr (D64) {
+        const double rd = (double)ri;
+        part = fma(rd, rd, part);
+      } else {
+        part32 = fmaf(ri, ri, part32);
+      }
     }
-    part = (double)part32;
+    if constexpr (!D64) part = (double)part32;
   }
   const double t = block_sum_staged<VEC_BLOCK>(part, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = t;
@@ -170,15 +178,18 @@ __global__ void __launch_bounds__(VEC_BLOCK) k_pupdate(T *__restrict__ p, const 
     p[i] = r[i] + b * p[i];
 }
 
-// partials of a . a, each thread's share in the vector's precision (see
-// k_update), the block sum in fp64
-template <typename T>
+// partials of a . a, each thread's share in FP64 (fp64 vectors, or D64)
+// or in the vector's precision (see k_update), the block sum in fp64
+template <typename T, bool D64>
 __global__ void __launch_bounds__(VEC_BLOCK) k_dot_self(const T *__restrict__ a, uint32_t n,
                                                         double *__restrict__ partials) {
   __shared__ double sh[VEC_BLOCK];
-  T part = T(0);
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    part = fma(a[i], a[i], part);
+  typedef typename std::conditional<sizeof(T) == 8 || D64, double, T>::type D;
+  D part = D(0);
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const D v = (D)a[i];
+    part = fma(v, v, part);
+  }
   const double t = block_sum_staged<VEC_BLOCK>((double)part, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = t;
 }
@@ -222,20 +233,25 @@ struct CgVectors {
   X *x, *r, *p, *q;
 };
 
-// One CG iteration; `parity` selects which rho slot is current.
+// One CG iteration; `parity` selects which rho slot is current.  d64: the
+// dot products p . q and r . r of FP32 vectors summed in FP64.
 template <typename X>
-void cg_iteration(const wk_engine *e, const CgVectors<X> &v, double *scal, double *partials, int parity,
+void cg_iteration(const wk_engine *e, const CgVectors<X> &v, double *scal, double *partials, int parity, bool d64,
                   cudaStream_t st) {
   const wk_layout *l = e->layout;
   const uint32_t W = l->info.nwarps, n = l->info.nrows;
   const unsigned g = spmv_dot_grid(l);
   const int i_rho = parity ? S_RHO1 : S_RHO0, i_next = parity ? S_RHO0 : S_RHO1;
   const int mode = short_layout(l, e->dtype) ? 2 : (e->compressed && e->dtype != WK_F64 ? 1 : 0);
-#define WK_SPMV_DOT1(V, M)                                                                                          \
-  k_spmv_dot<V, X, M><<<g, CG_BLOCK, 0, st>>>(e->vals.as<V>(), e->cols.as<int32_t>(), e->c16.as<uint16_t>(),      \
+#define WK_SPMV_DOT2(V, M, D)                                                                                       \
+  k_spmv_dot<V, X, M, D><<<g, CG_BLOCK, 0, st>>>(e->vals.as<V>(), e->cols.as<int32_t>(), e->c16.as<uint16_t>(),      \
                                                  e->c32.as<int32_t>(), e->cdesc.as<int4>(), l->d.warp_desc, W,        \
                                                  l->d.row_map, l->info.nznrows, n, v.p, v.q, scal, partials,       \
                                                  e->scale.as<float>())
+#define WK_SPMV_DOT1(V, M)                                                                                          \
+  do {                                                                                                              \
+    if (d64) WK_SPMV_DOT2(V, M, true); else WK_SPMV_DOT2(V, M, false);                                              \
+  } while (0)
 #define WK_SPMV_DOT(V)                                                                                              \
   do {                                                                                                              \
     if (mode == 2) WK_SPMV_DOT1(V, 2); else if (mode == 1) WK_SPMV_DOT1(V, 1); else WK_SPMV_DOT1(V, 0);             \
@@ -252,15 +268,22 @@ void cg_iteration(const wk_engine *e, const CgVectors<X> &v, double *scal, doubl
   }
 #undef WK_SPMV_DOT
 #undef WK_SPMV_DOT1
+#undef WK_SPMV_DOT2
   k_finish<false><<<1, 1024, 0, st>>>(partials, g, scal, S_PQ);
-  k_update<X><<<VEC_GRID, VEC_BLOCK, 0, st>>>(v.x, v.r, v.p, v.q, n, scal, i_rho, partials);
+  if (d64)
+    k_update<X, true><<<VEC_GRID, VEC_BLOCK, 0, st>>>(v.x, v.r, v.p, v.q, n, scal, i_rho, partials);
+  else
+    k_update<X, false><<<VEC_GRID, VEC_BLOCK, 0, st>>>(v.x, v.r, v.p, v.q, n, scal, i_rho, partials);
   k_finish<true><<<1, 1024, 0, st>>>(partials, VEC_GRID, scal, i_next);
   k_pupdate<X><<<VEC_GRID, VEC_BLOCK, 0, st>>>(v.p, v.r, n, scal, i_next, i_rho);
 }
 
 template <typename X>
-wk_status dot_self(const X *a, uint32_t n, double *partials, double *out, cudaStream_t st) {
-  k_dot_self<X><<<VEC_GRID, VEC_BLOCK, 0, st>>>(a, n, partials);
+wk_status dot_self(const X *a, uint32_t n, double *partials, double *out, bool d64, cudaStream_t st) {
+  if (d64)
+    k_dot_self<X, true><<<VEC_GRID, VEC_BLOCK, 0, st>>>(a, n, partials);
+  else
+    k_dot_self<X, false><<<VEC_GRID, VEC_BLOCK, 0, st>>>(a, n, partials);
   k_sum_to<<<1, 1024, 0, st>>>(partials, VEC_GRID, out);
   WK_CHECK_LAUNCH();
   return WK_OK;
@@ -275,10 +298,10 @@ struct IterGraph {
     if (cap) cudaStreamDestroy(cap);
   }
   template <typename X>
-  wk_status build(const wk_engine *e, const CgVectors<X> &v, double *scal, double *partials, int iters) {
+  wk_status build(const wk_engine *e, const CgVectors<X> &v, double *scal, double *partials, int iters, bool d64) {
     WK_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     WK_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-    for (int i = 0; i < iters; i++) cg_iteration<X>(e, v, scal, partials, i & 1, cap);
+    for (int i = 0; i < iters; i++) cg_iteration<X>(e, v, scal, partials, i & 1, d64, cap);
     cudaGraph_t g = nullptr;
     cudaError_t err = cudaStreamEndCapture(cap, &g);
     if (err != cudaSuccess) {
@@ -340,12 +363,12 @@ extern "C" wk_status wk_cg(wk_engine *e, const double *b, double *x, wk_cg_param
   double *scal = sb.as<double>(), *pp = part.as<double>();
   CgVectors<double> v{x, rb.as<double>(), pb.as<double>(), qb.as<double>()};
   IterGraph gr;
-  WK_TRY(gr.build<double>(e, v, scal, pp, batch_of(prm)));
+  WK_TRY(gr.build<double>(e, v, scal, pp, batch_of(prm), true));
   cudaEvent_t t0, t1;
   WK_CUDA(cudaEventCreate(&t0));
   WK_CUDA(cudaEventCreate(&t1));
   WK_CUDA(cudaEventRecord(t0, st));
-  WK_TRY(dot_self<double>(b, n, pp, scal + S_BB, st));
+  WK_TRY(dot_self<double>(b, n, pp, scal + S_BB, true, st));
   WK_TRY(launch_residual(e, x, b, v.r, pp, rg, scal + S_RHO0, st));
   WK_CUDA(cudaMemcpyAsync(v.p, v.r, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
   k_start<<<1, 1, 0, st>>>(scal, S_BB, prm->tol * prm->tol, (double)prm->max_iter);
@@ -398,13 +421,14 @@ extern "C" wk_status wk_ir_cg(wk_engine *e64, wk_engine *lo, const double *b, do
   WK_TRY(part.alloc(std::max(cg_partials(lo->layout, rg), cg_partials(e64->layout, rg)) * 8));
   double *r64 = r64b.as<double>(), *scal = sb.as<double>(), *pp = part.as<double>();
   CgVectors<float> v{db.as<float>(), r32b.as<float>(), pb.as<float>(), qb.as<float>()};
+  const bool d64 = prm->inner_dots_fp32 == 0;
   IterGraph gr;
-  WK_TRY(gr.build<float>(lo, v, scal, pp, batch_of(prm)));
+  WK_TRY(gr.build<float>(lo, v, scal, pp, batch_of(prm), d64));
   cudaEvent_t t0, t1;
   WK_CUDA(cudaEventCreate(&t0));
   WK_CUDA(cudaEventCreate(&t1));
   WK_CUDA(cudaEventRecord(t0, st));
-  WK_TRY(dot_self<double>(b, n, pp, scal + S_BB, st));
+  WK_TRY(dot_self<double>(b, n, pp, scal + S_BB, true, st));
   double bb = 0.0;
   WK_CUDA(cudaMemcpyAsync(&bb, scal + S_BB, 8, cudaMemcpyDeviceToHost, st));
   WK_CUDA(cudaStreamSynchronize(st));
@@ -420,7 +444,7 @@ extern "C" wk_status wk_ir_cg(wk_engine *e64, wk_engine *lo, const double *b, do
     if (!(rr64 > tol2) || outer >= prm->max_iter) break;
     // fp32 inner CG: A d = r from d = 0 until ||r_inner|| <= inner_tol ||r||
     k_ir_prepare<<<VEC_GRID, VEC_BLOCK, 0, st>>>(r64, v.r, v.x, v.p, n);
-    WK_TRY(dot_self<float>(v.r, n, pp, scal + S_RHO0, st));
+    WK_TRY(dot_self<float>(v.r, n, pp, scal + S_RHO0, d64, st));
     k_start<<<1, 1, 0, st>>>(scal, S_RHO0, inner_tol * inner_tol, (double)max_inner);
     WK_CHECK_LAUNCH();
     int its = 0, flag = 0;

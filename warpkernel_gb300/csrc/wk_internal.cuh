@@ -141,6 +141,10 @@ struct wk_engine {
   bool compressed = false;
   wk::DevBuf c16, c32, cdesc;
   wk::DevBuf scale;  // WK_F16S: float power-of-two scale per layout warp
+  // device address of wk_residual_static's static scratch array, looked up
+  // on the engine's first wk_residual_static call (an engine lives in one
+  // context, so the address stays valid for the engine's lifetime)
+  double *static_partials = nullptr;
 };
 
 namespace wk {

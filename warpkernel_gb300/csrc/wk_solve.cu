@@ -112,24 +112,23 @@ namespace {
 constexpr unsigned kResidualStaticBlocks = 65536;  // one double per block
 static __device__ __align__(256) double g_residual_partials[kResidualStaticBlocks];
 
-constexpr int kMaxDevices = 64;
-std::atomic<double *> g_residual_partials_addr[kMaxDevices];
-
-// Device address of g_residual_partials on the current device, looked up on
-// the first call per device (cudaGetSymbolAddress with that device current).
-wk_status static_partials(double **out) {
-  int dev = 0;
-  WK_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return set_error(WK_ERR_STATE, "device %d beyond the supported %d", dev, kMaxDevices);
-  double *p = g_residual_partials_addr[dev].load();
-  if (!p) {
-    cudaError_t e = cudaGetSymbolAddress((void **)&p, g_residual_partials);
-    if (e != cudaSuccess || !p)
-      return set_error(WK_ERR_CUDA, "cudaGetSymbolAddress(g_residual_partials) on device %d failed: %s", dev,
-                       cudaGetErrorString(e));
-    g_residual_partials_addr[dev].store(p);
+// Device address of g_residual_partials for engine e, looked up with
+// cudaGetSymbolAddress on the engine's first wk_residual_static call (with
+// the engine's device current, as for every call on the engine) and kept in
+// the engine.  Caching it per engine, not per device number, keeps it valid
+// across cudaDeviceReset: a reset frees the engine as well, and an engine
+// created afterwards looks the address up again in the new context.
+wk_status static_partials(wk_engine *e, double **out) {
+  if (!e->static_partials) {
+    double *p = nullptr;
+    cudaError_t err = cudaGetSymbolAddress((void **)&p, g_residual_partials);
+    if (err != cudaSuccess || !p) {
+      cudaGetLastError();
+      return set_error(WK_ERR_CUDA, "cudaGetSymbolAddress(g_residual_partials) failed: %s", cudaGetErrorString(err));
+    }
+    e->static_partials = p;
   }
-  *out = p;
+  *out = e->static_partials;
   return WK_OK;
 }
 }  // namespace
@@ -149,7 +148,7 @@ extern "C" wk_status wk_residual_static(wk_engine *e, const double *x, const dou
                      "scratch holds %u (at most %u layout warps); use wk_residual",
                      e->layout->info.nwarps, grid, kResidualStaticBlocks, kResidualStaticBlocks * (128u / 32u));
   double *partials = nullptr;
-  WK_TRY(static_partials(&partials));
+  WK_TRY(static_partials(e, &partials));
   return launch_residual(e, x, b, r, partials, grid, norm2, (cudaStream_t)stream);
 }
 

@@ -507,10 +507,15 @@ def cg(eng64, b, x, tol=1e-10, max_iter=100000, check_every=10, stream=None):
 
 
 def ir_cg(eng64, eng_lo, b, x, tol=1e-10, max_outer=50, max_inner=2000, inner_tol=1e-4, check_every=10,
-          stream=None):
+          stream=None, inner_dots="fp64"):
     """Iterative refinement: fp64 residual / dots / update, fp32 inner CG on
-    the low-precision engine (WK_F32 or WK_BF16 values)."""
+    the low-precision engine (WK_F32, WK_BF16 or WK_F16S values) whose dot
+    products are summed in FP64 (inner_dots="fp64") or in FP32 within each
+    block ("fp32")."""
+    if inner_dots not in ("fp64", "fp32"):
+        raise ValueError("inner_dots must be 'fp64' or 'fp32'")
     p = _cg_params(tol, max_outer, max_inner, inner_tol, check_every)
+    p.inner_dots_fp32 = 1 if inner_dots == "fp32" else 0
     st = load().wk_ir_cg(eng64.handle, eng_lo.handle, _ptr(b), _ptr(x), C.byref(p), _stream_ptr(stream))
     return _cg_result(p, st)
 
