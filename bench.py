@@ -341,15 +341,17 @@ def suite_mixed_and_cg(reps):
         e = wk.engine(k, fe.convert(vals, tdt), cols, dtype=dt)
         xd = fe.convert(x, tdt)
         yd = torch.zeros(n, dtype=torch.float32, device="cuda")
-        for comp in (False, True):
+        for comp, win in ((False, False), (True, False), (True, True)):
             if comp:
                 e.compress_cols()
+                nwin = e.set_windows(win)
             ms = _event_ms(lambda: e.run(0, 128, xd, yd, timed=False), reps)
             err = float(np.linalg.norm(yd.double().cpu().numpy() - y_ref) / np.linalg.norm(y_ref))
             ib = 2 if comp else 4
-            res["paths"][name + ("+cols16" if comp else "")] = {
+            res["paths"][name + ("+cols16" if comp else "") + ("+xwin" if win else "")] = {
                 "ms": round(ms, 4), "gnnz_s": round(nnz / ms / 1e6, 1), "speedup": round((nnz / ms) / base, 3),
-                "gbs": round(((vb + ib) * nnz + (xb + 4 + 4) * n) / ms / 1e6, 1), "rel_err": err}
+                "gbs": round(((vb + ib) * nnz + (xb + 4 + 4) * n) / ms / 1e6, 1), "rel_err": err,
+                **({"window_warps": nwin} if win else {})}
         engines[name] = e
     # CG: b = A x*, x* uniform(-1, 1)
     xs = fe.uniform_vec(2, 1, n)
@@ -470,7 +472,7 @@ def suite_adjoint(reps):
     return out
 
 
-def suite_f16s(reps, mesh=96, dtype="f16s", cols16=False):
+def suite_f16s(reps, mesh=96, dtype="f16s", cols16=False, windows=True):
     """hex mesh^3 (3 dof, seed 2, WPK2 threshold 81): one stored-value engine
     alone (`dtype` f16s: scaled FP16 values with FP32 x and y; f32; bf16 with
     bf16 x and FP32 y), optionally with 16-bit columns.  GB/s counts value +
@@ -487,15 +489,18 @@ def suite_f16s(reps, mesh=96, dtype="f16s", cols16=False):
     k = wk.structure2().scan(nnz, n, None, rp, None, 81)
     tdt, vb, xb = {"f16s": (torch.float32, 2, 4), "f32": (torch.float32, 4, 4), "bf16": (torch.bfloat16, 2, 2)}[dtype]
     e = wk.engine(k, fe.convert(vals, tdt), cols, dtype=dtype)
+    nwin = 0
     if cols16:
         e.compress_cols()
+        nwin = e.set_windows(windows)
     xd = fe.convert(x, tdt)
     yd = torch.zeros(n, dtype=torch.float32, device="cuda")
     ms = _event_ms(lambda: e.run(0, 128, xd, yd, timed=False), reps)
     y_ref = O.csr_spmv(rp.cpu().numpy(), cols.cpu().numpy(), vals.cpu().numpy(), x.cpu().numpy())
     err = float(np.linalg.norm(yd.double().cpu().numpy() - y_ref) / np.linalg.norm(y_ref))
     ib = 2 if cols16 else 4
-    return {"workload": f"hex{mesh}_3dof seed 2 {dtype}" + ("+cols16" if cols16 else ""), "nrows": n, "nnz": nnz,
+    return {"workload": f"hex{mesh}_3dof seed 2 {dtype}" + ("+cols16" if cols16 else "") + ("+xwin" if nwin else ""),
+            "window_warps": nwin, "nrows": n, "nnz": nnz,
             "ms": round(ms, 4), "gbs": round(((vb + ib) * nnz + (xb + 8) * n) / ms / 1e6, 1), "rel_err": err}
 
 
@@ -855,6 +860,7 @@ def main():
     ap.add_argument("--value-dtype", choices=["f16s", "f32", "bf16"], default="f16s",
                     help="--only f16s: the stored value type")
     ap.add_argument("--cols16", action="store_true", help="--only f16s: 16-bit column storage")
+    ap.add_argument("--no-windows", action="store_true", help="--only f16s: 16-bit columns without x windows")
     ap.add_argument("--only", choices=["mixed", "adjoint", "batched", "ablation", "cg", "f16s", "small", "permuted", "setup"],
                     help="run one suite alone (profiling cases; --steps = timed repetitions, "
                          "batched: the first 128 matrices with a fixed threshold / tile)")
@@ -872,7 +878,7 @@ def main():
         elif args.only == "cg":
             res = suite_cg(reps, args.mesh)
         elif args.only == "f16s":
-            res = suite_f16s(reps, args.mesh, args.value_dtype, args.cols16)
+            res = suite_f16s(reps, args.mesh, args.value_dtype, args.cols16, not args.no_windows)
         elif args.only == "small":
             res = suite_small()
         elif args.only == "permuted":

@@ -213,6 +213,22 @@ wk_status wk_engine_destroy(wk_engine *e);
  * rebuilds the compact storage. */
 wk_status wk_engine_compress_cols(wk_engine *e, void *stream, uint32_t *wide_warps);
 
+/* x windows (no reference counterpart; shared-memory staging of x in place of
+ * the reference's texture fetch, warpkernel.hpp:27-49), off by default.
+ * `on` = 1 (after wk_engine_compress_cols; WK_ERR_STATE otherwise) gives
+ * every narrow layout warp with at most 512 distinct columns, in at most 32
+ * chunks of <= 32 consecutive columns, an x window: its distinct columns as
+ * chunks, and per slot the window position of its column (2 B, a second
+ * per-slot array built on the first call).  Fast-order wk_run / wk_run_x then
+ * copy each such warp's x values into shared memory, one warp-wide load per
+ * chunk, and gather from there instead of from L1/L2; the sums are the same
+ * bits.  On GB300 this measured 1-8 % slower than the L1/L2 gathers for the
+ * 16-bit-column kernels (hex 96^3: the staging doubles the instructions of a
+ * warp's 2,500 slots while the gathers it replaces mostly hit L1), hence off.
+ * `on` = 0 switches them off again.  *window_warps (optional) = warps that
+ * have a window. */
+wk_status wk_engine_set_windows(wk_engine *e, int on, uint32_t *window_warps);
+
 /* ---- SpMV --------------------------------------------------------------- */
 
 /* Accumulation order of wk_run / wk_run_x. */

@@ -202,3 +202,40 @@ def test_fp32_storage_error_against_fp64():
             else:
                 # FP32 accumulation adds almost nothing to the rounding of the inputs
                 assert abs(err - input_err) < 0.05 * input_err, (order, err, input_err)
+
+
+@pytest.mark.parametrize("dtype", ["f32", "bf16", "f16s"])
+def test_x_windows_give_the_same_bits(dtype):
+    """Fast order with x windows staged in shared memory against the same
+    engine with the windows switched off: the same bits for run and run_x,
+    WPK1 and WPK2, block sizes of 1-32 warps (the 1,024-thread launch needs
+    more than 48 KB of shared memory); FE matrices give most warps a window,
+    random columns none."""
+    t = _t()
+    wk = _wk()
+    tdt = t.bfloat16 if dtype == "bf16" else t.float32
+    rng = np.random.default_rng(5)
+    cases = [("hex 10^3 x3", O.fe_matrix(3, 10, 10, 10, 3, value_mode=1, seed=3), True),
+             ("hex 6x7x40 x3", O.fe_matrix(3, 6, 7, 40, 3, value_mode=1, seed=4), True),
+             ("q1 90^2", O.fe_matrix(2, 90, 90, 0, 1, value_mode=0, seed=1), False),
+             ("random", random_csr(rng, 60_000, 90, p_empty=0.05), False)]
+    for name, (rp, cols, vals), fe in cases:
+        n = len(rp) - 1
+        x = wk.fe.convert(t.from_numpy(rng.uniform(-1, 1, n)).cuda(), tdt)
+        for kind, th in ((1, 0), (2, 40)):
+            k = wk.structure() if kind == 1 else wk.structure2()
+            k.scan(len(cols), n, None, rp, None, *(() if kind == 1 else (th,)))
+            eng = wk.engine(k, wk.fe.convert(t.from_numpy(vals).cuda(), tdt), t.from_numpy(cols).cuda(), dtype=dtype)
+            eng.compress_cols()
+            nwin = eng.set_windows(True)
+            if fe:
+                assert nwin >= 0.5 * k.nwarps, (name, kind, nwin, k.nwarps)
+            for bs in (32, 128, 1024):
+                for mapped in (True, False):
+                    out = {}
+                    for on in (True, False):
+                        eng.set_windows(on)
+                        y = t.zeros(n, dtype=t.float32, device="cuda")
+                        (eng.run if mapped else eng.run_x)(0, bs, x, y, order=0)
+                        out[on] = y
+                    assert t.equal(out[True], out[False]), (name, dtype, kind, bs, mapped)

@@ -66,6 +66,7 @@ SIGNATURES = {
     "wk_engine_get_colinds": (C.c_int, [vp, vp, C.c_size_t]),
     "wk_engine_destroy": (C.c_int, [vp]),
     "wk_engine_compress_cols": (C.c_int, [vp, vp, _u32p]),
+    "wk_engine_set_windows": (C.c_int, [vp, C.c_int, _u32p]),
     "wk_run": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, _fp]),
     "wk_run_x": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, _fp]),
     "wk_run_host": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, vp]),

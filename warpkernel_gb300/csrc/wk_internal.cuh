@@ -13,6 +13,11 @@
 
 namespace wk {
 
+// x windows (wk_compress.cu): at most WIN_MAX distinct columns in at most
+// WIN_CHUNKS chunks of <= 32 consecutive columns per layout warp.
+constexpr int WIN_MAX = 512;
+constexpr int WIN_CHUNKS = 32;
+
 // ---- errors ------------------------------------------------------------------
 wk_status set_error(wk_status code, const char *fmt, ...);
 const std::string &last_error();
@@ -140,6 +145,13 @@ struct wk_engine {
   // compact 32-bit indices of the warps whose span needs them, per-warp descriptor
   bool compressed = false;
   wk::DevBuf c16, c32, cdesc;
+  // x windows of the narrow warps (built with the compact columns): per slot
+  // the window position of its column, the chunks of each window, and per
+  // warp {first chunk, chunks (0: no window), window size, 0}
+  wk::DevBuf w16, wchunks, wdesc;
+  uint32_t window_warps = 0;
+  bool windows_built = false;
+  bool use_windows = false;  // wk_engine_set_windows (off by default: measured slower)
   wk::DevBuf scale;  // WK_F16S: float power-of-two scale per layout warp
   // device address of wk_residual_static's static scratch array, looked up
   // on the engine's first wk_residual_static call (an engine lives in one

@@ -92,21 +92,36 @@ __global__ void __launch_bounds__(1024) k_spmv_nocoal(const V *__restrict__ pv, 
   store_row<Acc, MAPPED>(y, row_map, p, s);
 }
 
-// Fast order with the 16-bit column storage of wk_engine_compress_cols.
-template <typename V, typename X, bool MAPPED, bool L1>
+// Fast order with the 16-bit column storage of wk_engine_compress_cols.  With
+// WIN (dynamic shared memory of WIN_MAX x values per warp of the block), the
+// warps that have an x window stage it in shared memory and gather from
+// there; the sums are the same bits as without.
+template <typename V, typename X, bool MAPPED, bool L1, bool WIN>
 __global__ void __launch_bounds__(1024) k_spmv_fast_c(const V *__restrict__ pv, const uint16_t *__restrict__ c16,
                                                       const int32_t *__restrict__ c32, const int4 *__restrict__ cdesc,
+                                                      const uint16_t *__restrict__ w16, const int2 *__restrict__ wch,
+                                                      const int4 *__restrict__ wdesc,
                                                       const int4 *__restrict__ desc, uint32_t W,
                                                       const int32_t *__restrict__ row_map, uint32_t nzr,
                                                       const X *__restrict__ x, typename Tr<V>::Acc *__restrict__ y,
                                                       const float *__restrict__ wscale) {
+  extern __shared__ __align__(16) unsigned char wk_dyn_smem[];
   const uint32_t lane = threadIdx.x & 31;
   const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
   if (w >= W) return;
   const int4 d = desc[w];
-  const int4 cd = cdesc[w];
   const uint32_t T = (uint32_t)d.z;
-  typename Tr<V>::Acc s = lane_sum_compressed<V, X, L1>(pv, c16, c32, d, cd, x, lane, policy_evict_first());
+  typename Tr<V>::Acc s;
+  const uint64_t pol = policy_evict_first();
+  int4 wd = make_int4(0, 0, 0, 0);
+  if constexpr (WIN) wd = wdesc[w];
+  if (WIN && wd.y != 0) {
+    X *win = reinterpret_cast<X *>(wk_dyn_smem) + (threadIdx.x / WS) * WIN_MAX;
+    stage_window<L1>(win, wch, wd, x, lane);
+    s = lane_sum_vec<V, X, L1, uint16_t, true, 0, true>(pv, w16 + (uint32_t)d.x, 0, d, win, lane, pol);
+  } else {
+    s = lane_sum_compressed<V, X, L1>(pv, c16, c32, d, cdesc[w], x, lane, pol);
+  }
   const uint32_t p = (uint32_t)d.w + lane / T;
   s = row_tree(s, T);
   if constexpr (Scaled<V>::value) s *= wscale[w];
@@ -146,12 +161,29 @@ wk_status dispatch(const RunArgs &a, unsigned grid, unsigned block) {
     const uint16_t *c16 = e->c16.as<uint16_t>();
     const int32_t *c32 = e->c32.as<int32_t>();
     const int4 *cd = e->cdesc.as<int4>();
-#define WK_LAUNCH_C(M, C) k_spmv_fast_c<V, X, M, C><<<grid, block, 0, a.stream>>>(pv, c16, c32, cd, desc, W, rm, nzr, x, y, ws)
+    const uint16_t *w16 = e->w16.as<uint16_t>();
+    const int2 *wch = e->wchunks.as<int2>();
+    const int4 *wd = e->wdesc.as<int4>();
+    const bool win = e->use_windows && e->windows_built && e->window_warps > 0;
+    const size_t smem = win ? (size_t)(block / WS) * WIN_MAX * sizeof(X) : 0;
+#define WK_LAUNCH_C(M, C, WN)                                                                              \
+  do {                                                                                                     \
+    if (smem > 48 * 1024)                                                                                  \
+      WK_CUDA(cudaFuncSetAttribute(k_spmv_fast_c<V, X, M, C, WN>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                   (int)smem));                                                            \
+    k_spmv_fast_c<V, X, M, C, WN><<<grid, block, smem, a.stream>>>(pv, c16, c32, cd, w16, wch, wd, desc, W, rm, \
+                                                                   nzr, x, y, ws);                         \
+  } while (0)
+#define WK_LAUNCH_CW(M, C)                                                                                 \
+  do {                                                                                                     \
+    if (win) WK_LAUNCH_C(M, C, true); else WK_LAUNCH_C(M, C, false);                                       \
+  } while (0)
     if (a.mapped) {
-      if (c) WK_LAUNCH_C(true, true); else WK_LAUNCH_C(true, false);
+      if (c) WK_LAUNCH_CW(true, true); else WK_LAUNCH_CW(true, false);
     } else {
-      if (c) WK_LAUNCH_C(false, true); else WK_LAUNCH_C(false, false);
+      if (c) WK_LAUNCH_CW(false, true); else WK_LAUNCH_CW(false, false);
     }
+#undef WK_LAUNCH_CW
 #undef WK_LAUNCH_C
     WK_CHECK_LAUNCH();
     return WK_OK;

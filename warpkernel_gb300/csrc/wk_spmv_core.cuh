@@ -106,6 +106,48 @@ __device__ __forceinline__ __nv_bfloat16 gather(const __nv_bfloat16 *x, int i) {
   return __ushort_as_bfloat16(L1 ? __ldg(u + i) : __ldca(u + i));
 }
 
+// x gather from global memory (gather<L1>) or, with SX, from an x window
+// staged in shared memory (stage_window): x then points at the window and i
+// is a window position.
+template <bool L1, bool SX, typename X>
+__device__ __forceinline__ X gx(const X *__restrict__ x, int i) {
+  if constexpr (SX)
+    return x[i];
+  else
+    return gather<L1>(x, i);
+}
+
+// Copies a layout warp's x window into shared memory `win` (the warp's
+// region, WIN_MAX values): wd = {first chunk, chunks, window size, 0}; chunk
+// q = {first column, window position | length << 16} holds at most 32
+// consecutive columns and is copied by one warp-wide load (lane j: column
+// first + j).  SW chunks' loads are issued before their stores, so a window
+// of up to SW chunks costs one round trip to L2.
+template <bool L1, typename X, int SW = 16>
+__device__ __forceinline__ void stage_window(X *win, const int2 *__restrict__ chunks, int4 wd,
+                                             const X *__restrict__ x, uint32_t lane) {
+  const int nch = wd.y;
+  const int2 mine = lane < (uint32_t)nch ? chunks[wd.x + lane] : make_int2(0, 0);
+  for (int q0 = 0; q0 < nch; q0 += SW) {
+    X v[SW];
+    int dst[SW];
+#pragma unroll
+    for (int j = 0; j < SW; j++) {
+      const int q = q0 + j;
+      const int c0 = __shfl_sync(0xffffffffu, mine.x, q & 31);
+      const int pl = __shfl_sync(0xffffffffu, mine.y, q & 31);
+      const int pos = (pl & 0xffff) + (int)lane;
+      const bool ok = q < nch && lane < (uint32_t)(pl >> 16) && pos < WIN_MAX;
+      dst[j] = ok ? pos : -1;
+      v[j] = ok ? gather<L1>(x, c0 + (int)lane) : X(0.0f);
+    }
+#pragma unroll
+    for (int j = 0; j < SW; j++)
+      if (dst[j] >= 0) win[dst[j]] = v[j];
+  }
+  __syncwarp();
+}
+
 __device__ __forceinline__ double fma_acc(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float fma_acc(float a, float b, float c) { return fmaf(a, b, c); }
 
@@ -306,8 +348,9 @@ __device__ __forceinline__ T block_sum_staged(T v, T *sh) {
 // cp0 points at the warp's first column entry (slot o_w of a slot-indexed
 // array, or the warp's start in a compact array); base is added to 16-bit
 // offsets.
-// UNR (if non-zero) replaces the plan's unroll factor.
-template <typename V, typename X, bool L1, typename C, bool TUNED = true, int UNR = 0>
+// UNR (if non-zero) replaces the plan's unroll factor.  SX: x is the warp's
+// x window in shared memory and the columns are window positions (base 0).
+template <typename V, typename X, bool L1, typename C, bool TUNED = true, int UNR = 0, bool SX = false>
 __device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict__ pv, const C *__restrict__ cp0, int base,
                                                            int4 d, const X *__restrict__ x, uint32_t lane,
                                                            uint64_t pol) {
@@ -338,7 +381,7 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict_
       }
 #pragma unroll
       for (int k = 0; k < S; k++)
-        a[k] = fma_acc(Tr<V>::acc(word_val<V>(wv, k)), (Acc)Tr<X>::acc(gather<L1>(x, word_col<C>(wc, k, base))), a[k]);
+        a[k] = fma_acc(Tr<V>::acc(word_val<V>(wv, k)), (Acc)Tr<X>::acc(gx<L1, SX>(x, word_col<C>(wc, k, base))), a[k]);
 #pragma unroll
       for (int q = 0; q < NWV; q++) wv[q] = nv[q];
 #pragma unroll
@@ -355,7 +398,7 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict_
     ld_words(cp, wc, pol);
 #pragma unroll
     for (int k = 0; k < S; k++)
-      a[k] = fma_acc(Tr<V>::acc(word_val<V>(wv, k)), (Acc)Tr<X>::acc(gather<L1>(x, word_col<C>(wc, k, base))), a[k]);
+      a[k] = fma_acc(Tr<V>::acc(word_val<V>(wv, k)), (Acc)Tr<X>::acc(gx<L1, SX>(x, word_col<C>(wc, k, base))), a[k]);
     vp += S * WS;
     cp += S * WS;
   }
@@ -377,7 +420,7 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict_
       if ((uint32_t)i < rem) {
         const size_t k = ut + (size_t)i * WS;
         tv[i] = Tr<V>::acc(ld_stream1(pv + o + k, pol));
-        tx[i] = (Acc)Tr<X>::acc(gather<L1>(x, ld_col1(cp0 + k, base, pol)));
+        tx[i] = (Acc)Tr<X>::acc(gx<L1, SX>(x, ld_col1(cp0 + k, base, pol)));
       }
     }
     Acc s = combine_lanes<S>(a, lane);
@@ -389,7 +432,7 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict_
     Acc s = combine_lanes<S>(a, lane);
     for (uint32_t i = 0; i < rem; i++) {
       const int c = ld_col1(cp0 + ut + (size_t)i * WS, base, pol);
-      s = fma_acc(Tr<V>::acc(ld_stream1(pv + o + ut + (size_t)i * WS, pol)), (Acc)Tr<X>::acc(gather<L1>(x, c)), s);
+      s = fma_acc(Tr<V>::acc(ld_stream1(pv + o + ut + (size_t)i * WS, pol)), (Acc)Tr<X>::acc(gx<L1, SX>(x, c)), s);
     }
     return s;
   } else {
@@ -400,7 +443,7 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict_
     Acc tail = Acc(0);
     for (uint32_t i = 0; i < rem; i++) {
       const int c = ld_col1(cp0 + ut + (size_t)i * WS, base, pol);
-      tail = fma_acc(Tr<V>::acc(ld_stream1(pv + o + ut + (size_t)i * WS, pol)), (Acc)Tr<X>::acc(gather<L1>(x, c)), tail);
+      tail = fma_acc(Tr<V>::acc(ld_stream1(pv + o + ut + (size_t)i * WS, pol)), (Acc)Tr<X>::acc(gx<L1, SX>(x, c)), tail);
     }
     return combine_lanes<S>(a, lane) + tail;
   }

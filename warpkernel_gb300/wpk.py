@@ -354,6 +354,13 @@ class engine:
         check(load().wk_engine_compress_cols(self.handle, _stream_ptr(stream), C.byref(wide)))
         return int(wide.value)
 
+    def set_windows(self, on=True):
+        """x windows of the compact column storage on or off (fast order; the
+        same bits either way); returns the number of warps that have one."""
+        n = C.c_uint32(0)
+        check(load().wk_engine_set_windows(self.handle, int(bool(on)), C.byref(n)))
+        return int(n.value)
+
     def set_values(self, A, stream=None):
         check(load().wk_engine_set_values(self.handle, _ptr(A), _stream_ptr(stream)))
 
