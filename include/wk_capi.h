@@ -449,10 +449,15 @@ typedef struct wk_batch wk_batch;
  * computes them. */
 wk_status wk_batch_create(wk_engine *const *engines, const uint32_t *nrhs, int count, int rhs_tile, int chunk,
                           wk_batch **out);
-/* X[m]: device, ncols_m x nrhs_m, row-major; Y[m]: device, nrows_m x nrhs_m
- * (rows without entries are not written).  WK_F32 rows of X whose length is a
- * multiple of 4 (X[m] 16-byte aligned) are gathered with 16-byte loads and run
- * about 1.4x faster per right-hand side than other lengths. */
+/* X[m]: device, ncols_m x nrhs_m, row-major, any alignment of the element
+ * type; Y[m]: device, nrows_m x nrhs_m (rows without entries are not
+ * written).  The batch keeps a blocked copy of X -- the right-hand sides in
+ * groups of 16 bytes (4 floats / 2 doubles, zero-filled), each group an
+ * ncols_m x group array -- which every launch refreshes from X[m] before the
+ * SpMV, so every right-hand-side count is gathered with 16-byte loads (device
+ * memory: ncols_m x nrhs_m rounded up to the group, per matrix).  Call again
+ * (and wk_batch_capture again) when X or Y move; WK_ERR_INVALID if a
+ * matrix's blocked X would hold 2^32 elements or more. */
 wk_status wk_batch_set_vectors(wk_batch *b, const void *const *X, void *const *Y);
 wk_status wk_batch_set_tile(wk_batch *b, int rhs_tile);
 /* Captures the launch (queue reset + persistent kernel) into a CUDA graph

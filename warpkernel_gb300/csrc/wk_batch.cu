@@ -6,8 +6,8 @@
 // the next item from a global counter.  Which warp computes an item does not
 // change its arithmetic, so results are deterministic.  For each stored slot
 // the value and column are loaded once and reused for an RHS tile of TR
-// right-hand sides: X is row-major (ncols x k), so the TR values of column c
-// are contiguous and are gathered with vector loads.  The counter reset and
+// right-hand sides, gathered with 16-byte loads from a blocked copy of X
+// (see Blk) that each launch writes first.  The counter reset, the copy and
 // the kernel are captured once in a CUDA graph and replayed.
 #include <algorithm>
 #include <cstring>
@@ -26,35 +26,102 @@ constexpr int WS = 32;
 #endif
 constexpr int BATCH_BLOCK = WK_BATCH_BLOCK;
 
+// X is gathered from a blocked copy: right-hand sides BW*b .. BW*b+BW-1
+// (BW = 16 bytes of T: 4 floats or 2 doubles) of every column form block b,
+// an ncols x BW row-major array, zero-filled beyond the last right-hand side.
+// A warp's gather of one block then reads 16 bytes per lane from rows of 16
+// bytes: the 32 lanes, whose columns are neighbours in a finite-element
+// matrix, touch about 512 contiguous bytes (4 L1 lines) per load instead of
+// 32 rows of the caller's k-wide layout (up to 2 KB, 16 lines for k = 16;
+// scalar loads when k is not a multiple of 4), which was the L1 wavefront
+// limit of the kernel.  k_xblock writes the blocked copy at the start of
+// every launch.
+template <typename T>
+struct Blk {
+  static constexpr int BW = 16 / (int)sizeof(T);
+  typedef typename std::conditional<sizeof(T) == 4, float4, double2>::type V;
+};
+
 template <typename T>
 struct BatchMat {
   const int4 *desc;
   const T *vals;
   const int32_t *cols;
   const int32_t *row_map;
-  const T *X;
-  T *Y;
-  uint32_t nzr, W, k, ld;  // ld = row stride of X and Y (= k)
+  const T *Xb;  // blocked X: block b at Xb + b * ncols * BW
+  T *Y;         // caller's Y, nrows x k row-major
+  uint32_t nzr, W, k, ncols;
 };
 
+// One item of the blocked copy: rows [r0, r1) of one matrix's X.
+template <typename T>
+struct XCopy {
+  const T *X;
+  T *Xb;
+  uint32_t ncols, k, r0, r1;
+};
+
+__device__ __forceinline__ void set_vec(float (&g)[4], const float4 f) {
+  g[0] = f.x; g[1] = f.y; g[2] = f.z; g[3] = f.w;
+}
+__device__ __forceinline__ void set_vec(double (&g)[2], const double2 f) {
+  g[0] = f.x; g[1] = f.y;
+}
+
+// g = the TR right-hand sides j0 .. j0+TR-1 of column c (zeros from jn on).
+// xt = the tile's first block plus j0 % BW (Xb + (j0 / BW) * bstride +
+// j0 % BW), bstride = ncols * BW elements; a matrix's blocked X holds fewer
+// than 2^32 elements (wk_batch_set_vectors checks), so offsets fit 32 bits.
 template <typename T, int TR>
-__device__ __forceinline__ void gather_tile(const T *__restrict__ xr, int jn, bool vec4, T (&g)[TR]) {
-  if constexpr (TR >= 4 && sizeof(T) == 4) {
-    if (vec4) {
+__device__ __forceinline__ void gather_tile(const T *__restrict__ xt, uint32_t c, uint32_t bstride, int jn,
+                                            T (&g)[TR]) {
+  constexpr int BW = Blk<T>::BW;
+  typedef typename Blk<T>::V V;
+  const T *xc = xt + (size_t)c * BW;
+  if constexpr (TR >= BW) {
 #pragma unroll
-      for (int j = 0; j < TR; j += 4) {
-        if (j < jn) {
-          const float4 f = __ldg(reinterpret_cast<const float4 *>(xr + j));
-          g[j] = f.x; g[j + 1] = f.y; g[j + 2] = f.z; g[j + 3] = f.w;
-        } else {
-          g[j] = g[j + 1] = g[j + 2] = g[j + 3] = T(0);
-        }
+    for (int j = 0; j < TR; j += BW) {
+      T q[BW];
+      if (j < jn)
+        set_vec(q, __ldg(reinterpret_cast<const V *>(xc + (uint32_t)(j / BW) * bstride)));
+      else
+#pragma unroll
+        for (int i = 0; i < BW; i++) q[i] = T(0);
+#pragma unroll
+      for (int i = 0; i < BW; i++) g[j + i] = q[i];
+    }
+  } else {  // the tile lies inside one block
+#pragma unroll
+    for (int j = 0; j < TR; j++) g[j] = j < jn ? __ldg(xc + j) : T(0);
+  }
+}
+
+// The blocked copy of X: one block of threads per item, thread i of a row
+// range handles (row r0 + i / nb, block i % nb).
+template <typename T>
+__global__ void __launch_bounds__(256) k_xblock(const XCopy<T> *__restrict__ items, uint32_t nitems) {
+  constexpr int BW = Blk<T>::BW;
+  typedef typename Blk<T>::V V;
+  for (uint32_t it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const XCopy<T> c = items[it];
+    const uint32_t nb = (c.k + BW - 1) / BW;
+    const size_t n = (size_t)(c.r1 - c.r0) * nb;
+    for (size_t i = threadIdx.x; i < n; i += blockDim.x) {
+      const uint32_t r = c.r0 + (uint32_t)(i / nb), b = (uint32_t)(i % nb);
+      T q[BW];
+#pragma unroll
+      for (int t = 0; t < BW; t++) {
+        const uint32_t j = (uint32_t)BW * b + (uint32_t)t;
+        q[t] = j < c.k ? __ldg(c.X + (size_t)r * c.k + j) : T(0);
       }
-      return;
+      V v;
+      if constexpr (BW == 4)
+        v = make_float4(q[0], q[1], q[2], q[3]);
+      else
+        v = make_double2(q[0], q[1]);
+      *reinterpret_cast<V *>(c.Xb + ((size_t)b * c.ncols + r) * BW) = v;
     }
   }
-#pragma unroll
-  for (int j = 0; j < TR; j++) g[j] = j < jn ? __ldg(xr + j) : T(0);
 }
 
 // Value / column words of one unit of S steps (S slots of 32 B per lane).
@@ -109,8 +176,8 @@ __global__ void __launch_bounds__(BATCH_BLOCK, (batch_min_blocks<T, TR>())) k_ba
     if (it >= nitems) break;
     const int4 item = items[it];
     const BatchMat<T> M = mats[item.x];
-    const uint32_t k = M.k, ld = M.ld;
-    const bool vec4 = (ld & 3u) == 0 && ((reinterpret_cast<uintptr_t>(M.X) & 15u) == 0);
+    const uint32_t k = M.k;
+    const uint32_t bstride = M.ncols * (uint32_t)Blk<T>::BW;
     for (uint32_t w = (uint32_t)item.y; w < (uint32_t)item.z; w++) {
       const int4 d = M.desc[w];
       const uint32_t T_ = (uint32_t)d.z, A = (uint32_t)d.y;
@@ -120,6 +187,7 @@ __global__ void __launch_bounds__(BATCH_BLOCK, (batch_min_blocks<T, TR>())) k_ba
       const uint32_t units = A / S, rem = A % S;
       for (uint32_t j0 = 0; j0 < k; j0 += TR) {
         const int jn = (int)min((uint32_t)TR, k - j0);
+        const T *xt = M.Xb + (size_t)(j0 / Blk<T>::BW) * bstride + (j0 % Blk<T>::BW);
         T acc[TR];
 #pragma unroll
         for (int j = 0; j < TR; j++) acc[j] = T(0);
@@ -147,7 +215,7 @@ __global__ void __launch_bounds__(BATCH_BLOCK, (batch_min_blocks<T, TR>())) k_ba
             const int q = st * WS + (int)lane;
             const T v = staged_val<T>(sv, q);
             T g[TR];
-            gather_tile<T, TR>(M.X + (size_t)sc[q] * ld + j0, jn, vec4, g);
+            gather_tile<T, TR>(xt, (uint32_t)sc[q], bstride, jn, g);
 #pragma unroll
             for (int j = 0; j < TR; j++) acc[j] = fma(v, g[j], acc[j]);
           }
@@ -157,7 +225,7 @@ __global__ void __launch_bounds__(BATCH_BLOCK, (batch_min_blocks<T, TR>())) k_ba
           const T v = __ldcs(M.vals + slot);
           const int c = __ldcs(M.cols + slot);
           T g[TR];
-          gather_tile<T, TR>(M.X + (size_t)c * ld + j0, jn, vec4, g);
+          gather_tile<T, TR>(xt, (uint32_t)c, bstride, jn, g);
 #pragma unroll
           for (int j = 0; j < TR; j++) acc[j] = fma(v, g[j], acc[j]);
         }
@@ -165,7 +233,7 @@ __global__ void __launch_bounds__(BATCH_BLOCK, (batch_min_blocks<T, TR>())) k_ba
         for (int j = 0; j < TR; j++)
           for (uint32_t s2 = 1; s2 < T_; s2 <<= 1) acc[j] += __shfl_down_sync(0xffffffffu, acc[j], s2);
         if (valid && (lane & (T_ - 1)) == 0) {
-          T *yr = M.Y + (size_t)M.row_map[p] * ld + j0;
+          T *yr = M.Y + (size_t)M.row_map[p] * k + j0;
 #pragma unroll
           for (int j = 0; j < TR; j++)
             if (j < jn) __stcs(yr + j, acc[j]);  // streaming: keeps X in L2 (1.5 % faster)
@@ -186,7 +254,8 @@ struct wk_batch {
   std::vector<uint32_t> nrhs;
   std::vector<uint32_t> nrows, ncols;
   wk::DevBuf mats, items, counter;
-  uint32_t nitems = 0;
+  wk::DevBuf xb, xcopy;  // blocked X of every matrix, and the copy items
+  uint32_t nitems = 0, ncopy = 0;
   unsigned grid = 0;
   bool vectors_set = false;
   cudaGraphExec_t graph = nullptr;
@@ -218,7 +287,46 @@ wk_status launch_batch_t(wk_batch *b, cudaStream_t st) {
 
 wk_status launch_batch(wk_batch *b, cudaStream_t st) {
   WK_CUDA(cudaMemsetAsync(b->counter.p, 0, sizeof(unsigned), st));
+  if (b->ncopy) {
+    const unsigned g = std::min<unsigned>(b->ncopy, 152u * 8u);
+    if (b->dtype == WK_F64)
+      k_xblock<double><<<g, 256, 0, st>>>(b->xcopy.as<XCopy<double>>(), b->ncopy);
+    else
+      k_xblock<float><<<g, 256, 0, st>>>(b->xcopy.as<XCopy<float>>(), b->ncopy);
+    WK_CHECK_LAUNCH();
+  }
   return b->dtype == WK_F64 ? launch_batch_t<double>(b, st) : launch_batch_t<float>(b, st);
+}
+
+// The blocked X buffer (one region per matrix, 16-byte aligned) and the copy
+// items (rows of one matrix, XCOPY_ROWS at a time), for the caller's X.
+constexpr uint32_t XCOPY_ROWS = 2048;
+template <typename T>
+wk_status setup_blocked_x(wk_batch *b, const void *const *X, std::vector<size_t> &off) {
+  constexpr int BW = Blk<T>::BW;
+  const size_t n = b->engines.size();
+  off.assign(n, 0);
+  size_t total = 0;
+  std::vector<XCopy<T>> items;
+  for (size_t m = 0; m < n; m++) {
+    const size_t nb = (b->nrhs[m] + BW - 1) / BW;
+    if (nb * (size_t)b->ncols[m] * BW >= ((size_t)1 << 32))
+      return set_error(WK_ERR_INVALID, "matrix %zu: ncols x right-hand sides (%u x %u) too large for a batch", m,
+                       b->ncols[m], b->nrhs[m]);
+    off[m] = total;
+    total += nb * (size_t)b->ncols[m] * BW;  // elements; a multiple of BW (16 bytes)
+  }
+  WK_TRY(b->xb.alloc(total * sizeof(T)));
+  T *base = b->xb.as<T>();
+  for (size_t m = 0; m < n; m++)
+    for (uint32_t r0 = 0; r0 < b->ncols[m]; r0 += XCOPY_ROWS)
+      items.push_back({(const T *)X[m], base + off[m], b->ncols[m], b->nrhs[m], r0,
+                       std::min(b->ncols[m], r0 + XCOPY_ROWS)});
+  WK_TRY(b->xcopy.alloc(items.size() * sizeof(XCopy<T>)));
+  if (!items.empty())
+    WK_CUDA(cudaMemcpy(b->xcopy.p, items.data(), items.size() * sizeof(XCopy<T>), cudaMemcpyHostToDevice));
+  b->ncopy = (uint32_t)items.size();
+  return WK_OK;
 }
 
 template <typename T>
@@ -330,22 +438,28 @@ extern "C" wk_status wk_batch_create(wk_engine *const *engines, const uint32_t *
 extern "C" wk_status wk_batch_set_vectors(wk_batch *b, const void *const *X, void *const *Y) {
   if (!b || !X || !Y) return set_error(WK_ERR_INVALID, "NULL argument");
   const size_t n = b->engines.size();
+  for (size_t m = 0; m < n; m++)
+    if (!X[m] || !Y[m]) return set_error(WK_ERR_INVALID, "matrix %zu: NULL X or Y", m);
+  drop_graph(b);
+  std::vector<size_t> off;
   if (b->dtype == WK_F64) {
+    WK_TRY(setup_blocked_x<double>(b, X, off));
     std::vector<BatchMat<double>> h(n);
     for (size_t m = 0; m < n; m++) {
       const wk_engine *e = b->engines[m];
       h[m] = {e->layout->d.warp_desc, e->vals.as<double>(), e->cols.as<int32_t>(), e->layout->d.row_map,
-              (const double *)X[m], (double *)Y[m], e->layout->info.nznrows, e->layout->info.nwarps, b->nrhs[m],
-              b->nrhs[m]};
+              b->xb.as<double>() + off[m], (double *)Y[m], e->layout->info.nznrows, e->layout->info.nwarps,
+              b->nrhs[m], b->ncols[m]};
     }
     WK_CUDA(cudaMemcpy(b->mats.p, h.data(), n * sizeof(h[0]), cudaMemcpyHostToDevice));
   } else {
+    WK_TRY(setup_blocked_x<float>(b, X, off));
     std::vector<BatchMat<float>> h(n);
     for (size_t m = 0; m < n; m++) {
       const wk_engine *e = b->engines[m];
       h[m] = {e->layout->d.warp_desc, e->vals.as<float>(), e->cols.as<int32_t>(), e->layout->d.row_map,
-              (const float *)X[m], (float *)Y[m], e->layout->info.nznrows, e->layout->info.nwarps, b->nrhs[m],
-              b->nrhs[m]};
+              b->xb.as<float>() + off[m], (float *)Y[m], e->layout->info.nznrows, e->layout->info.nwarps,
+              b->nrhs[m], b->ncols[m]};
     }
     WK_CUDA(cudaMemcpy(b->mats.p, h.data(), n * sizeof(h[0]), cudaMemcpyHostToDevice));
   }
