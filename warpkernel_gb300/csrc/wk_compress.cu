@@ -280,8 +280,11 @@ unsigned grid_for_warps(uint32_t W) {
 }  // namespace
 
 // Builds the x windows of an engine with compact columns (see above).
-wk_status build_windows(wk_engine *e, cudaStream_t st) {
-  const wk_layout *l = e->layout;
+// x windows of layout l over its padded columns `cols` (device), given the
+// per-warp modes / bases of k_col_modes in `cdesc`: the slots' window
+// positions (w16), the chunks and the per-warp window descriptors.
+wk_status build_window_arrays(const wk_layout *l, const int32_t *cols, const int4 *cdesc, DevBuf &w16,
+                              DevBuf &wchunks, DevBuf &wdesc, uint32_t *warps, cudaStream_t st) {
   const uint32_t W = l->info.nwarps;
   const size_t anz = l->info.allocate_nz;
   DevBuf tot;
@@ -291,34 +294,51 @@ wk_status build_windows(wk_engine *e, cudaStream_t st) {
   WK_TRY(choff.alloc((size_t)W * 8));
   if (W) {
     const unsigned g = (unsigned)std::min<size_t>(W, 152u * 8u);
-    k_win_count<<<g, WB, 0, st>>>(l->d.warp_desc, W, l->d.slen, l->info.nznrows, e->cols.as<int32_t>(),
-                                  e->cdesc.as<int4>(), nch.as<unsigned long long>());
+    k_win_count<<<g, WB, 0, st>>>(l->d.warp_desc, W, l->d.slen, l->info.nznrows, cols, cdesc,
+                                  nch.as<unsigned long long>());
     WK_CHECK_LAUNCH();
   }
   WK_TRY(scan_u64(nch.as<unsigned long long>(), choff.as<unsigned long long>(), W, tot.as<unsigned long long>(), st));
   unsigned long long nchunks = 0;
   WK_CUDA(cudaMemcpyAsync(&nchunks, tot.p, 8, cudaMemcpyDeviceToHost, st));
   WK_CUDA(cudaStreamSynchronize(st));
-  WK_TRY(e->wchunks.alloc(nchunks * 8));
-  WK_TRY(e->wdesc.alloc((size_t)W * sizeof(int4)));
-  WK_TRY(e->w16.alloc(anz * 2));
+  WK_TRY(wchunks.alloc(nchunks * 8));
+  WK_TRY(wdesc.alloc((size_t)W * sizeof(int4)));
+  WK_TRY(w16.alloc(anz * 2));
   if (W) {
     const unsigned g = (unsigned)std::min<size_t>(W, 152u * 8u);
-    k_win_fill<<<g, WB, 0, st>>>(l->d.warp_desc, W, l->d.slen, l->info.nznrows, e->cols.as<int32_t>(),
-                                 e->cdesc.as<int4>(), nch.as<unsigned long long>(), choff.as<unsigned long long>(),
-                                 e->wdesc.as<int4>(), e->wchunks.as<int2>(), e->w16.as<uint16_t>());
+    k_win_fill<<<g, WB, 0, st>>>(l->d.warp_desc, W, l->d.slen, l->info.nznrows, cols, cdesc,
+                                 nch.as<unsigned long long>(), choff.as<unsigned long long>(), wdesc.as<int4>(),
+                                 wchunks.as<int2>(), w16.as<uint16_t>());
     WK_CHECK_LAUNCH();
   }
   WK_CUDA(cudaStreamSynchronize(st));
-  {
-    std::vector<unsigned long long> h(W);
-    if (W) WK_CUDA(cudaMemcpy(h.data(), nch.p, (size_t)W * 8, cudaMemcpyDeviceToHost));
-    uint32_t c = 0;
-    for (unsigned long long v : h) c += v != 0;
-    e->window_warps = c;
-  }
+  std::vector<unsigned long long> h(W);
+  if (W) WK_CUDA(cudaMemcpy(h.data(), nch.p, (size_t)W * 8, cudaMemcpyDeviceToHost));
+  uint32_t c = 0;
+  for (unsigned long long v : h) c += v != 0;
+  *warps = c;
+  return WK_OK;
+}
+
+wk_status build_windows(wk_engine *e, cudaStream_t st) {
+  WK_TRY(build_window_arrays(e->layout, e->cols.as<int32_t>(), e->cdesc.as<int4>(), e->w16, e->wchunks, e->wdesc,
+                             &e->window_warps, st));
   e->windows_built = true;
   return WK_OK;
+}
+
+wk_status build_window_set(const wk_layout *l, const int32_t *cols, WinSet &ws, cudaStream_t st) {
+  const uint32_t W = l->info.nwarps;
+  DevBuf wide;
+  WK_TRY(ws.cdesc.alloc((size_t)W * sizeof(int4)));
+  WK_TRY(wide.alloc((size_t)W * 8));
+  if (W) {
+    k_col_modes<<<grid_for_warps(W), 256, 0, st>>>(l->d.warp_desc, W, l->d.slen, l->info.nznrows, cols,
+                                                   ws.cdesc.as<int4>(), wide.as<unsigned long long>());
+    WK_CHECK_LAUNCH();
+  }
+  return build_window_arrays(l, cols, ws.cdesc.as<int4>(), ws.w16, ws.chunks, ws.wdesc, &ws.warps, st);
 }
 
 wk_status build_compressed_cols(wk_engine *e, cudaStream_t st, uint32_t *wide_warps) {

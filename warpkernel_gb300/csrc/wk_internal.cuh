@@ -203,6 +203,14 @@ wk_status make_engine(wk_layout *l, int dtype, const void *d_vals, const int32_t
 wk_status load_values(wk_engine *e, const void *d_vals, cudaStream_t stream);
 // WK_F16S: decodes the padded values to FP32 (allocate_nz floats, device).
 wk_status launch_f16s_decode(const wk_engine *e, float *out, cudaStream_t stream);
+// x windows of a layout over padded device columns, owned by the caller
+// (the adjoint's): per-warp modes / bases, slot window positions, chunks and
+// window descriptors (see wk_compress.cu).
+struct WinSet {
+  DevBuf cdesc, w16, chunks, wdesc;
+  uint32_t warps = 0;
+};
+wk_status build_window_set(const wk_layout *l, const int32_t *cols, WinSet &ws, cudaStream_t stream);
 // Builds / refreshes the engine's 16-bit column storage from its int32 columns.
 wk_status build_compressed_cols(wk_engine *e, cudaStream_t stream, uint32_t *wide_warps);
 
