@@ -146,10 +146,10 @@ __global__ void k_dvals_slots(const int4 *__restrict__ desc, uint32_t W, const i
 // 128-bit accesses despite the lower occupancy).  dvals go to the same slots
 // with one vector store per lane, or (CSR order) through shared memory, which
 // measured 11 % faster (fp32) than the 4-slot kernel it replaced.  It serves
-// fp64, CSR order and 16-bit columns; the fp32 slot-order gradient on 32-bit
-// columns runs k_adjoint_sym_staged (below), 6 % faster at hex 64^3 (0.133
-// against 0.1415 ms), where this kernel stays ahead for fp64 (0.262 against
-// 0.264 ms staged, 0.289 with x windows).
+// fp64 and CSR order; the fp32 slot-order gradient runs k_adjoint_sym_staged
+// (below), 0.114 against 0.1415 ms at hex 64^3.  For fp64 this kernel stayed
+// ahead of a register-staged form of that kernel (0.262 against 0.264 ms,
+// 0.289 with x windows).
 template <typename T>
 struct AdjSlots {
   static constexpr int value = core::SlotsPerLane<T>::value;
@@ -411,21 +411,42 @@ __global__ void __launch_bounds__(AdjCfg<T, CSR>::warps * 32, AdjCfg<T, CSR>::mi
     dx[row_map[q]] = T(0);
 }
 
-// Fused slot-order adjoint with the matrix stream staged through shared
-// memory: each unit of S steps is loaded with one 32-byte load of mirror
-// values and one load of columns per lane, stored to the warp's tile and
-// read back step by step, so lane l handles its own layout lane: dx
-// accumulates in one register in step order (no cross-lane combine), the
-// row's dy and slot count stay in registers, and each step's 32 gradients
-// leave in one coalesced 128-byte store.  WIN: the warp has an x window
-// (WinSet): its (x, dy) pairs are first copied into shared memory (one
-// warp-wide load per chunk of <= 32 consecutive columns), the stream carries
-// 16-bit window positions instead of 32-bit columns, and every gather reads
-// shared memory.
-// Six blocks of 4 warps per SM (80 registers, 24 KB of shared memory each):
-// 0.133 ms at hex 64^3 against 0.140-0.144 with four, five or seven blocks.
-constexpr int ADJ_SW = 4;  // warps per block of the staged kernel
-constexpr int ADJ_STAGED_BLOCKS = 6;
+// Fused slot-order adjoint with the matrix stream copied into shared memory
+// (fp32, 32-bit columns).  Each unit of S steps of mirror values and
+// columns is copied by cp.async (16 bytes per lane and instruction, L2
+// evict-first) into a ring of STAGES tiles, STAGES - 1 units ahead, and read
+// back step by step, so lane l handles its own layout lane: dx accumulates in
+// one register in step order (no cross-lane combine), the row's dy and slot
+// count stay in registers, and each step's 32 gradients leave in one
+// coalesced 128-byte streaming store.  WIN: the warp has an x window
+// (WinSet): its (x, dy) pairs are copied into shared memory by the same
+// asynchronous copies (issued with the first unit, so their L2 latency
+// overlaps the stream's), the stream carries 16-bit window positions instead
+// of 32-bit columns, and every gather reads shared memory.  XD: x and dy are
+// read from their own vectors (every warp has a window, so no interleaved
+// copy is needed).  Measured at hex 64^3 (fp32): 0.119 ms against 0.133 with
+// the units staged through registers and 0.1415 for k_adjoint_sym_slots;
+// two to four stages and five to seven blocks per SM within 1 %.
+constexpr int ADJ_SW = 4;          // warps per block
+constexpr int ADJ_STAGES = 3;      // tiles in the ring
+constexpr int ADJ_STAGED_BLOCKS = 5;
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, uint64_t pol) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(sa), "l"(gmem), "l"(pol)
+               : "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_ca(void *smem, const void *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(sa), "l"(gmem), "n"(N) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 // XD: x and dy read from their own vectors (no interleaved copy).
 template <typename T, bool XD>
 __device__ __forceinline__ typename Pair<T>::type pair_at(const typename Pair<T>::type *__restrict__ xdy,
@@ -440,91 +461,98 @@ __device__ __forceinline__ typename Pair<T>::type pair_at(const typename Pair<T>
   }
 }
 
-template <typename T, bool WIN, bool XD>
-__device__ __forceinline__ T adjoint_warp_staged(const int4 d, const int32_t *__restrict__ pc,
-                                                 const uint16_t *__restrict__ w16, const T *__restrict__ tv,
-                                                 const typename Pair<T>::type *__restrict__ xdy,
-                                                 const T *__restrict__ x, const T *__restrict__ dy,
-                                                 const typename Pair<T>::type *wp, T *__restrict__ dvals, uint32_t *sv,
-                                                 int32_t *sc, T dyr, int el, uint32_t lane, uint64_t pol) {
+template <bool WIN, bool XD>
+__device__ __forceinline__ float adjoint_warp_pipe(const int4 d, const int4 wd, const int2 *__restrict__ wch,
+                                                   const int32_t *__restrict__ pc, const uint16_t *__restrict__ w16,
+                                                   const float *__restrict__ tv, const float2 *__restrict__ xdy,
+                                                   const float *__restrict__ x, const float *__restrict__ dy,
+                                                   float2 *wp, float *__restrict__ dvals, uint32_t *sv, int32_t *sc,
+                                                   float dyr, int el, uint32_t lane, uint64_t pol) {
   using namespace core;
-  typedef typename Pair<T>::type P;
-  constexpr int S = 32 / (int)sizeof(T);       // steps per unit: 8 fp32, 4 fp64
-  constexpr int NV = S * (int)sizeof(T) / 4;   // value words per lane and unit
-  constexpr int NC = WIN ? S / 2 : S;          // column words per lane and unit
+  constexpr int S = 8;                 // steps per unit (32 bytes of fp32 per lane)
+  constexpr int NC = WIN ? S / 2 : S;  // column words per lane and unit
+  constexpr int VSTAGE = S * WS, CSTAGE = S * WS;  // words per tile
   const size_t o = (size_t)(uint32_t)d.x;
   const uint32_t A = (uint32_t)d.y, units = A / S, rem = A % S;
-  T acc = T(0);
-  uint32_t wv[NV], wc[NC];
-  if (units) {
-    ld_words(tv + o + S * lane, wv, pol);
-    if constexpr (WIN)
-      ld_words(w16 + o + S * lane, wc, pol);
-    else
-      ld_words(pc + o + S * lane, wc, pol);
+  auto issue = [&](uint32_t u) {
+    const size_t g = o + (size_t)u * S * WS + S * lane;
+    uint32_t *dv = sv + (u % ADJ_STAGES) * VSTAGE + S * lane;
+#pragma unroll
+    for (int q = 0; q < S; q += 4) cp_async16(dv + q, tv + g + q, pol);
+    uint32_t *dc = reinterpret_cast<uint32_t *>(sc) + (u % ADJ_STAGES) * CSTAGE + NC * lane;
+    const uint32_t *gc = WIN ? reinterpret_cast<const uint32_t *>(w16 + g) : reinterpret_cast<const uint32_t *>(pc + g);
+#pragma unroll
+    for (int q = 0; q < NC; q += 4) cp_async16(dc + q, gc + q, pol);
+  };
+  // group 0: the first unit and the window's (x, dy) pairs; then units 1 ..
+  // STAGES - 2, one group each
+  if (units) issue(0);
+  if constexpr (WIN) {
+    // chunk q = {first column, window position | length << 16}, <= 32 columns
+    const int nch = wd.y;
+    const int2 mine = lane < (uint32_t)nch ? wch[wd.x + lane] : make_int2(0, 0);
+    for (int q = 0; q < nch; q++) {
+      const int c0 = __shfl_sync(0xffffffffu, mine.x, q);
+      const int pl = __shfl_sync(0xffffffffu, mine.y, q);
+      const int pos = (pl & 0xffff) + (int)lane;
+      if (lane < (uint32_t)(pl >> 16) && pos < WIN_MAX) {
+        if constexpr (XD) {
+          cp_async_ca<4>(&wp[pos].x, x + c0 + (int)lane);
+          cp_async_ca<4>(&wp[pos].y, dy + c0 + (int)lane);
+        } else {
+          cp_async_ca<8>(&wp[pos], xdy + c0 + (int)lane);
+        }
+      }
+    }
   }
+  cp_async_commit();
+#pragma unroll
+  for (int s = 1; s < ADJ_STAGES - 1; s++) {
+    if ((uint32_t)s < units) issue((uint32_t)s);
+    cp_async_commit();
+  }
+  float acc = 0.f;
   for (uint32_t u = 0; u < units; u++) {
+    if (u + ADJ_STAGES - 1 < units) issue(u + ADJ_STAGES - 1);
+    cp_async_commit();
+    cp_async_wait<ADJ_STAGES - 1>();
     __syncwarp();
-#pragma unroll
-    for (int q = 0; q < NV; q += 4)
-      *reinterpret_cast<uint4 *>(sv + NV * lane + q) = make_uint4(wv[q], wv[q + 1], wv[q + 2], wv[q + 3]);
-    // columns (or packed 16-bit window positions) in slot order, one
-    // conflict-free 16-byte store per 4 words
-    if constexpr (NC % 4 == 0) {
-#pragma unroll
-      for (int q = 0; q < NC; q += 4)
-        *reinterpret_cast<uint4 *>(reinterpret_cast<uint32_t *>(sc) + NC * lane + q) =
-            make_uint4(wc[q], wc[q + 1], wc[q + 2], wc[q + 3]);
-    } else {
-#pragma unroll
-      for (int q = 0; q < NC; q += 2)
-        *reinterpret_cast<uint2 *>(reinterpret_cast<uint32_t *>(sc) + NC * lane + q) = make_uint2(wc[q], wc[q + 1]);
-    }
-    __syncwarp();
-    if (u + 1 < units) {
-      const size_t nxt = o + (size_t)(u + 1) * S * WS + S * lane;
-      ld_words(tv + nxt, wv, pol);
-      if constexpr (WIN)
-        ld_words(w16 + nxt, wc, pol);
-      else
-        ld_words(pc + nxt, wc, pol);
-    }
-    T *dp = dvals + o + (size_t)u * S * WS + lane;
+    const uint32_t *svs = sv + (u % ADJ_STAGES) * VSTAGE;
+    const int32_t *scs = sc + (u % ADJ_STAGES) * CSTAGE;
+    float *dp = dvals + o + (size_t)u * S * WS + lane;
 #pragma unroll
     for (int st = 0; st < S; st++) {
       const int q = st * WS + (int)lane;
-      T v;
-      if constexpr (sizeof(T) == 4)
-        v = __uint_as_float(sv[q]);
-      else
-        v = __hiloint2double((int)sv[2 * q + 1], (int)sv[2 * q]);
-      const P g = WIN ? wp[reinterpret_cast<const uint16_t *>(sc)[q]] : pair_at<T, XD>(xdy, x, dy, sc[q]);
-      acc = fma(v, g.y, acc);
-      __stcs(dp + st * WS, (int)(u * S + st) < el ? dyr * g.x : T(0));
+      const float v = __uint_as_float(svs[q]);
+      const float2 g = WIN ? wp[reinterpret_cast<const uint16_t *>(scs)[q]] : pair_at<float, XD>(xdy, x, dy, scs[q]);
+      acc = fmaf(v, g.y, acc);
+      __stcs(dp + st * WS, (int)(u * S + st) < el ? dyr * g.x : 0.f);
     }
+    __syncwarp();  // this tile is refilled STAGES - 1 units later
   }
+  cp_async_wait<0>();
+  __syncwarp();  // the window of a warp without a full unit
   size_t slot = o + (size_t)units * S * WS + lane;
   for (uint32_t i = 0; i < rem; i++, slot += WS) {
-    const P g = WIN ? wp[ld_col1(w16 + slot, 0, pol)] : pair_at<T, XD>(xdy, x, dy, __ldcs(pc + slot));
-    acc = fma(__ldcs(tv + slot), g.y, acc);
-    __stcs(dvals + slot, (int)(units * S + i) < el ? dyr * g.x : T(0));
+    const float2 g = WIN ? wp[ld_col1(w16 + slot, 0, pol)] : pair_at<float, XD>(xdy, x, dy, __ldcs(pc + slot));
+    acc = fmaf(__ldcs(tv + slot), g.y, acc);
+    __stcs(dvals + slot, (int)(units * S + i) < el ? dyr * g.x : 0.f);
   }
   return acc;
 }
 
-template <typename T, bool WIN, bool XD>
+template <bool WIN, bool XD>
 __global__ void __launch_bounds__(ADJ_SW * 32, ADJ_STAGED_BLOCKS) k_adjoint_sym_staged(
     const int4 *__restrict__ desc, uint32_t W, const int32_t *__restrict__ row_map, const uint32_t *__restrict__ slen,
     uint32_t nzr, uint32_t nrows, const int32_t *__restrict__ pc, const uint16_t *__restrict__ w16,
-    const int2 *__restrict__ wch, const int4 *__restrict__ wdesc, const T *__restrict__ tv,
-    const typename Pair<T>::type *__restrict__ xdy, const T *__restrict__ x, const T *__restrict__ dy,
-    T *__restrict__ dx, T *__restrict__ dvals) {
+    const int2 *__restrict__ wch, const int4 *__restrict__ wdesc, const float *__restrict__ tv,
+    const float2 *__restrict__ xdy, const float *__restrict__ x, const float *__restrict__ dy, float *__restrict__ dx,
+    float *__restrict__ dvals) {
   using namespace core;
-  typedef typename Pair<T>::type P;
-  constexpr int S = 32 / (int)sizeof(T);
-  __shared__ __align__(16) uint32_t s_val[ADJ_SW][S * WS * (int)sizeof(T) / 4];
-  __shared__ __align__(16) int32_t s_col[ADJ_SW][S * WS];
-  __shared__ __align__(16) P s_win[WIN ? ADJ_SW : 1][WIN ? WIN_MAX : 1];
+  constexpr int S = 8;
+  __shared__ __align__(16) uint32_t s_val[ADJ_SW][ADJ_STAGES * S * WS];
+  __shared__ __align__(16) int32_t s_col[ADJ_SW][ADJ_STAGES * S * WS];
+  __shared__ __align__(16) float2 s_win[WIN ? ADJ_SW : 1][WIN ? WIN_MAX : 1];
   const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x / WS;
   const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
   if (w < W) {
@@ -535,53 +563,26 @@ __global__ void __launch_bounds__(ADJ_SW * 32, ADJ_STAGED_BLOCKS) k_adjoint_sym_
     const bool valid = p < nzr;
     int32_t row = 0;
     int el = 0;
-    T dyr = T(0);
+    float dyr = 0.f;
     if (valid) {
       row = row_map[p];
       el = max(0, min((int)A, (int)slen[p] - (int)(t * A)));
       dyr = XD ? dy[row] : xdy[row].y;
     }
-    T acc;
-    bool staged = false;
-    if constexpr (WIN) {
-      const int4 wd = wdesc[w];
-      if (wd.y != 0) {
-        // the window's (x, dy) pairs: chunk q = {first column, position | length << 16}
-        P *wp = s_win[wib];
-        const int nch = wd.y;
-        const int2 mine = lane < (uint32_t)nch ? wch[wd.x + lane] : make_int2(0, 0);
-        for (int q0 = 0; q0 < nch; q0 += 8) {
-          P v[8];
-          int dst[8];
-#pragma unroll
-          for (int j = 0; j < 8; j++) {
-            const int q = q0 + j;
-            const int c0 = __shfl_sync(0xffffffffu, mine.x, q & 31);
-            const int pl = __shfl_sync(0xffffffffu, mine.y, q & 31);
-            const int pos = (pl & 0xffff) + (int)lane;
-            const bool ok = q < nch && lane < (uint32_t)(pl >> 16) && pos < WIN_MAX;
-            dst[j] = ok ? pos : -1;
-            if (ok) v[j] = pair_at<T, XD>(xdy, x, dy, c0 + (int)lane);
-          }
-#pragma unroll
-          for (int j = 0; j < 8; j++)
-            if (dst[j] >= 0) wp[dst[j]] = v[j];
-        }
-        __syncwarp();
-        acc = adjoint_warp_staged<T, true, XD>(d, pc, w16, tv, xdy, x, dy, wp, dvals, s_val[wib], s_col[wib], dyr, el,
-                                               lane, pol);
-        staged = true;
-      }
-    }
-    if (!staged)
-      acc = adjoint_warp_staged<T, false, XD>(d, pc, w16, tv, xdy, x, dy, nullptr, dvals, s_val[wib], s_col[wib], dyr,
-                                              el, lane, pol);
+    const int4 wd = WIN ? wdesc[w] : make_int4(0, 0, 0, 0);
+    const float acc0 =
+        (WIN && wd.y != 0)
+            ? adjoint_warp_pipe<WIN, XD>(d, wd, wch, pc, w16, tv, xdy, x, dy, s_win[wib], dvals, s_val[wib],
+                                         s_col[wib], dyr, el, lane, pol)
+            : adjoint_warp_pipe<false, XD>(d, wd, wch, pc, w16, tv, xdy, x, dy, nullptr, dvals, s_val[wib], s_col[wib],
+                                           dyr, el, lane, pol);
+    float acc = acc0;
     for (uint32_t k = 1; k < T_; k <<= 1) acc += __shfl_down_sync(0xffffffffu, acc, k);
     if (valid && (lane & (T_ - 1)) == 0) dx[row] = acc;
   }
   for (size_t q = (size_t)nzr + (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < nrows;
        q += (size_t)gridDim.x * blockDim.x)
-    dx[row_map[q]] = T(0);
+    dx[row_map[q]] = 0.f;
 }
 
 wk_status refresh_transposed(wk_adjoint *a, const void *vals_csr, cudaStream_t st) {
@@ -753,23 +754,24 @@ extern "C" wk_status wk_adjoint_run(wk_adjoint *a, const void *x, const void *dy
     if (slots && ((uintptr_t)dvals & 31u))
       return set_error(WK_ERR_INVALID, "slot-order dvals must be 32-byte aligned");
     const unsigned gi = grid_for(n, 256);
-    // fp32 gradient in slot order on 32-bit columns: the staged kernel, with
-    // the x windows of the forward layout (built on the first such call)
-    if (!f64 && slots && !f->compressed) {
+    // fp32 gradient in slot order: the staged kernel, with the x windows of
+    // the forward layout's int32 columns (built on the first such call; the
+    // forward engine's own 16-bit columns, if any, are not used here)
+    if (!f64 && slots) {
       if (!a->win_built) {
         WK_TRY(build_window_set(L, f->cols.as<int32_t>(), a->win, st));
         a->win_built = true;
       }
       const unsigned g = (unsigned)std::max<size_t>(1, ((size_t)W + ADJ_SW - 1) / ADJ_SW);
       if (a->win.warps == W) {  // every warp stages its window: x and dy read directly
-        k_adjoint_sym_staged<float, true, true><<<g, ADJ_SW * 32, 0, st>>>(
+        k_adjoint_sym_staged<true, true><<<g, ADJ_SW * 32, 0, st>>>(
             L->d.warp_desc, W, L->d.row_map, L->d.slen, L->info.nznrows, n, f->cols.as<int32_t>(),
             a->win.w16.as<uint16_t>(), a->win.chunks.as<int2>(), a->win.wdesc.as<int4>(), a->te->vals.as<float>(),
             nullptr, (const float *)x, (const float *)dy, (float *)dx, (float *)dvals);
       } else {
         if (a->xdy.bytes < pb) WK_TRY(a->xdy.alloc(pb));
         k_interleave<float><<<gi, 256, 0, st>>>((const float *)x, (const float *)dy, n, a->xdy.as<float2>());
-        k_adjoint_sym_staged<float, true, false><<<g, ADJ_SW * 32, 0, st>>>(
+        k_adjoint_sym_staged<true, false><<<g, ADJ_SW * 32, 0, st>>>(
             L->d.warp_desc, W, L->d.row_map, L->d.slen, L->info.nznrows, n, f->cols.as<int32_t>(),
             a->win.w16.as<uint16_t>(), a->win.chunks.as<int2>(), a->win.wdesc.as<int4>(), a->te->vals.as<float>(),
             a->xdy.as<float2>(), nullptr, nullptr, (float *)dx, (float *)dvals);
