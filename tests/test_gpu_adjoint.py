@@ -344,3 +344,87 @@ def test_gradient_at_benchmark_size_hex64(value_order):
                             for r in touched)
         fd = (tot[1] - tot[-1]) / (2 * h)
         assert abs(fd - dx[i]) <= 1e-7 * max(abs(fd), 1e-3), (i, fd, dx[i])
+
+
+def _periodic_band(n, length):
+    """Pattern-symmetric CSR with every row of `length` entries: row i holds
+    columns (i + k) mod n for k in -h..h (odd length, with the diagonal) or
+    k in -h..h without 0 (even length).  Rows of equal length keep their
+    index order in the layout, so every warp's columns form one or two runs."""
+    h = length // 2
+    ks = [k for k in range(-h, h + 1) if length % 2 or k != 0]
+    cols = np.sort((np.arange(n)[:, None] + np.array(ks)[None, :]) % n, axis=1)
+    rp = np.arange(n + 1, dtype=np.int32) * len(ks)
+    return rp, cols.reshape(-1).astype(np.int32)
+
+
+def _check_fp32_slot_gradient(rp, cols, vals, kind, th, rng):
+    """fp32 slot-order fused adjoint against the host: dvals bit-identical to
+    the fp32 products dy[row] x[col], padding slots 0, dx within 1e-5 of the
+    fp64 transpose product of the same fp32 inputs."""
+    import torch
+
+    from warpkernel_gb300.autograd import WPKMatrix
+    n = len(rp) - 1
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    vh = vals.astype(np.float32)
+    xh = rng.uniform(-1, 1, n).astype(np.float32)
+    dyh = rng.uniform(-1, 1, n).astype(np.float32)
+    m_csr = WPKMatrix(rp, cols, torch.from_numpy(vh), kind=kind, threshold=th)
+    assert m_csr.symmetric
+    v = torch.from_numpy(vh).cuda()
+    mat = WPKMatrix(rp, cols, m_csr.to_slots(v), kind=kind, threshold=th, value_order="slots")
+    dx, dv = mat.adjoint(torch.from_numpy(xh).cuda(), torch.from_numpy(dyh).cuda())
+    pad = torch.ones(mat.allocate_nz, dtype=torch.bool, device="cuda")
+    pad[mat._reorder_rows()] = False
+    assert not torch.any(dv[pad] != 0)
+    assert np.array_equal(mat.to_csr(dv).cpu().numpy(), dyh[rows] * xh[cols])
+    dx_ref = O.csr_spmv_t(rp, cols, vh.astype(np.float64), dyh.astype(np.float64), n)
+    assert rel(dx.double().cpu().numpy(), dx_ref) < 1e-5
+
+
+def test_fp32_slot_order_every_remainder():
+    """The fp32 slot-order kernel streams units of 8 steps and a partial last
+    unit through its shared-memory ring: constant row lengths 1-20 and 40
+    (every remainder modulo 8, zero to five full units) in WPK1, and WPK2
+    with a threshold that splits the rows; n = 1000 leaves a partial last
+    warp.  Every warp of these bands has an x window."""
+    rng = np.random.default_rng(23)
+    for length in list(range(1, 21)) + [40]:
+        rp, cols = _periodic_band(1000, length)
+        vals = rng.standard_normal(len(cols))
+        _check_fp32_slot_gradient(rp, cols, vals, 1, None, rng)
+        if length >= 6:
+            _check_fp32_slot_gradient(rp, cols, vals, 2, 4, rng)
+
+
+def test_fp32_slot_order_mixed_windows():
+    """A band whose rows 300-499 also hold 24 random far columns (mirrored,
+    so the pattern stays symmetric): their warps see hundreds of distinct
+    columns and have no x window, the band's warps keep theirs, and the
+    kernel's window and plain-gather paths run side by side."""
+    rng = np.random.default_rng(29)
+    n = 2000
+    rp0, cols0 = _periodic_band(n, 13)
+    rows0 = np.repeat(np.arange(n), np.diff(rp0))
+    far_r = np.repeat(np.arange(300, 500), 24)
+    far_c = rng.integers(0, n, far_r.size)
+    r = np.concatenate([rows0, far_r, far_c]).astype(np.int64)
+    c = np.concatenate([cols0, far_c, far_r]).astype(np.int64)
+    key = np.unique(r * n + c)
+    r, c = key // n, key % n
+    rp = np.zeros(n + 1, np.int64)
+    np.add.at(rp, r + 1, 1)
+    rp = np.cumsum(rp).astype(np.int32)
+    vals = rng.standard_normal(len(c))
+    for kind, th in ((1, None), (2, 8)):
+        _check_fp32_slot_gradient(rp, c.astype(np.int32), vals, kind, th, rng)
+
+
+def test_fp32_slot_order_at_benchmark_size_hex64():
+    """The differentiable-SpMV benchmark's own path: hex 64^3, 3 dof (seed 4),
+    fp32 values, WPK2 threshold 81, gradient in slot order."""
+    from warpkernel_gb300 import fe
+    rp_d, cols_d, vals_d = fe.fe_matrix(3, 64, 64, 64, 3, 1, 4)
+    rp, cols, vals = rp_d.cpu().numpy(), cols_d.cpu().numpy(), vals_d.cpu().numpy()
+    _check_fp32_slot_gradient(rp, cols, vals, 2, 81, np.random.default_rng(64))

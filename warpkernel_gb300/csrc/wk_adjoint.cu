@@ -412,24 +412,26 @@ __global__ void __launch_bounds__(AdjCfg<T, CSR>::warps * 32, AdjCfg<T, CSR>::mi
 }
 
 // Fused slot-order adjoint with the matrix stream copied into shared memory
-// (fp32, 32-bit columns).  Each unit of S steps of mirror values and
-// columns is copied by cp.async (16 bytes per lane and instruction, L2
-// evict-first) into a ring of STAGES tiles, STAGES - 1 units ahead, and read
-// back step by step, so lane l handles its own layout lane: dx accumulates in
-// one register in step order (no cross-lane combine), the row's dy and slot
-// count stay in registers, and each step's 32 gradients leave in one
-// coalesced 128-byte streaming store.  WIN: the warp has an x window
-// (WinSet): its (x, dy) pairs are copied into shared memory by the same
-// asynchronous copies (issued with the first unit, so their L2 latency
-// overlaps the stream's), the stream carries 16-bit window positions instead
-// of 32-bit columns, and every gather reads shared memory.  XD: x and dy are
-// read from their own vectors (every warp has a window, so no interleaved
-// copy is needed).  Measured at hex 64^3 (fp32): 0.119 ms against 0.133 with
-// the units staged through registers and 0.1415 for k_adjoint_sym_slots;
-// two to four stages and five to seven blocks per SM within 1 %.
-constexpr int ADJ_SW = 4;          // warps per block
-constexpr int ADJ_STAGES = 3;      // tiles in the ring
-constexpr int ADJ_STAGED_BLOCKS = 5;
+// (fp32).  Each unit of S steps of mirror values and columns is copied by
+// cp.async (16 bytes per lane and instruction, L2 evict-first) into a ring
+// of STAGES tiles, STAGES - 1 units ahead, and read back step by step, so
+// lane l handles its own layout lane: dx accumulates in one register in step
+// order (no cross-lane combine), the row's dy and slot count stay in
+// registers, and each step's 32 gradients leave in one coalesced 128-byte
+// streaming store.  A warp with an x window (WinSet) copies its (x, dy)
+// pairs into shared memory with the first unit's copies (so their L2
+// latency overlaps the stream's), streams 16-bit window positions instead of
+// 32-bit columns, and gathers from shared memory; a warp without one gathers
+// x and dy from their vectors.  Full units run an unguarded step loop (a
+// guard per step for the partial last unit cost 21 % more instructions and
+// 7 % of the time).  Measured at hex 64^3 (fp32, three of 25,747 layout warps
+// without a window): 0.105 ms with four stages and four blocks per SM,
+// against 0.1415 for k_adjoint_sym_slots; three stages 0.106, two 0.109.
+// A persistent form (each warp walking layout warps gw, gw +
+// NW, ... with the ring and a double-buffered window running on across
+// them, so that no layout warp's descriptor and window latency is exposed)
+// measured 0.123-0.129 ms: the second window buffer costs a block per SM.
+constexpr int ADJ_SW = 4;  // warps per block
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem, uint64_t pol) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
@@ -447,46 +449,58 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// XD: x and dy read from their own vectors (no interleaved copy).
-template <typename T, bool XD>
-__device__ __forceinline__ typename Pair<T>::type pair_at(const typename Pair<T>::type *__restrict__ xdy,
-                                                          const T *__restrict__ x, const T *__restrict__ dy, int c) {
-  if constexpr (XD) {
-    typename Pair<T>::type g;
-    g.x = __ldg(x + c);
-    g.y = __ldg(dy + c);
-    return g;
-  } else {
-    return __ldg(xdy + c);
-  }
-}
-
-template <bool WIN, bool XD>
+// One layout warp.  Units of S steps; the last unit may be partial (the
+// remainder steps ride in the same ring, copied by the lanes that hold
+// them).  The first STAGES - 1 units are issued as soon as the descriptors
+// are known, before the row data and the window, which join the first
+// group.  WIN: the warp has an x window (its (x, dy) pairs staged in `wp`,
+// the stream carries 16-bit window positions); otherwise the stream carries
+// 32-bit columns and x, dy are gathered from their vectors.
+template <int STAGES, bool WIN>
 __device__ __forceinline__ float adjoint_warp_pipe(const int4 d, const int4 wd, const int2 *__restrict__ wch,
                                                    const int32_t *__restrict__ pc, const uint16_t *__restrict__ w16,
-                                                   const float *__restrict__ tv, const float2 *__restrict__ xdy,
-                                                   const float *__restrict__ x, const float *__restrict__ dy,
-                                                   float2 *wp, float *__restrict__ dvals, uint32_t *sv, int32_t *sc,
-                                                   float dyr, int el, uint32_t lane, uint64_t pol) {
+                                                   const float *__restrict__ tv, const float *__restrict__ x,
+                                                   const float *__restrict__ dy, const int32_t *__restrict__ row_map,
+                                                   const uint32_t *__restrict__ slen, uint32_t nzr, float2 *wp,
+                                                   float *__restrict__ dvals, uint32_t *sv, uint32_t *sc,
+                                                   uint32_t lane, uint64_t pol, int32_t &row, bool &valid) {
   using namespace core;
   constexpr int S = 8;                 // steps per unit (32 bytes of fp32 per lane)
   constexpr int NC = WIN ? S / 2 : S;  // column words per lane and unit
-  constexpr int VSTAGE = S * WS, CSTAGE = S * WS;  // words per tile
+  constexpr int VSTAGE = S * WS, CSTAGE = NC * WS;  // words per tile
   const size_t o = (size_t)(uint32_t)d.x;
-  const uint32_t A = (uint32_t)d.y, units = A / S, rem = A % S;
+  const uint32_t A = (uint32_t)d.y, full = A / S, rem = A % S, units = full + (rem != 0);
+  // unit u covers steps [u S, u S + S) of all lanes: S * 32 consecutive
+  // slots, of which lane l copies S (and NC column words) from S l on; in a
+  // partial unit only the lanes below 4 rem hold slots
   auto issue = [&](uint32_t u) {
-    const size_t g = o + (size_t)u * S * WS + S * lane;
-    uint32_t *dv = sv + (u % ADJ_STAGES) * VSTAGE + S * lane;
+    if (u < full || lane < 4 * rem) {
+      const size_t g = o + (size_t)u * S * WS + S * lane;
+      uint32_t *dv = sv + (u % STAGES) * VSTAGE + S * lane;
 #pragma unroll
-    for (int q = 0; q < S; q += 4) cp_async16(dv + q, tv + g + q, pol);
-    uint32_t *dc = reinterpret_cast<uint32_t *>(sc) + (u % ADJ_STAGES) * CSTAGE + NC * lane;
-    const uint32_t *gc = WIN ? reinterpret_cast<const uint32_t *>(w16 + g) : reinterpret_cast<const uint32_t *>(pc + g);
+      for (int q = 0; q < S; q += 4) cp_async16(dv + q, tv + g + q, pol);
+      uint32_t *dc = sc + (u % STAGES) * CSTAGE + NC * lane;
+      const uint32_t *gc =
+          WIN ? reinterpret_cast<const uint32_t *>(w16 + g) : reinterpret_cast<const uint32_t *>(pc + g);
 #pragma unroll
-    for (int q = 0; q < NC; q += 4) cp_async16(dc + q, gc + q, pol);
+      for (int q = 0; q < NC; q += 4) cp_async16(dc + q, gc + q, pol);
+    }
   };
-  // group 0: the first unit and the window's (x, dy) pairs; then units 1 ..
-  // STAGES - 2, one group each
-  if (units) issue(0);
+#pragma unroll
+  for (int s = 0; s < STAGES - 1; s++)
+    if ((uint32_t)s < units) issue((uint32_t)s);
+  // the lane's row: its dy and slot count
+  const uint32_t T_ = (uint32_t)d.z, t = lane % T_;
+  const uint32_t p = (uint32_t)d.w + lane / T_;
+  valid = p < nzr;
+  row = 0;
+  int el = 0;
+  float dyr = 0.f;
+  if (valid) {
+    row = row_map[p];
+    el = max(0, min((int)A, (int)slen[p] - (int)(t * A)));
+    dyr = dy[row];
+  }
   if constexpr (WIN) {
     // chunk q = {first column, window position | length << 16}, <= 32 columns
     const int nch = wd.y;
@@ -496,87 +510,81 @@ __device__ __forceinline__ float adjoint_warp_pipe(const int4 d, const int4 wd, 
       const int pl = __shfl_sync(0xffffffffu, mine.y, q);
       const int pos = (pl & 0xffff) + (int)lane;
       if (lane < (uint32_t)(pl >> 16) && pos < WIN_MAX) {
-        if constexpr (XD) {
-          cp_async_ca<4>(&wp[pos].x, x + c0 + (int)lane);
-          cp_async_ca<4>(&wp[pos].y, dy + c0 + (int)lane);
-        } else {
-          cp_async_ca<8>(&wp[pos], xdy + c0 + (int)lane);
-        }
+        cp_async_ca<4>(&wp[pos].x, x + c0 + (int)lane);
+        cp_async_ca<4>(&wp[pos].y, dy + c0 + (int)lane);
       }
     }
   }
-  cp_async_commit();
+  // group 0: units 0 .. STAGES - 2 and the window; groups 1 .. STAGES - 2
+  // are empty, so that group u is complete once STAGES - 1 later ones are
+  // committed
 #pragma unroll
-  for (int s = 1; s < ADJ_STAGES - 1; s++) {
-    if ((uint32_t)s < units) issue((uint32_t)s);
-    cp_async_commit();
-  }
+  for (int s = 0; s < STAGES - 1; s++) cp_async_commit();
   float acc = 0.f;
   for (uint32_t u = 0; u < units; u++) {
-    if (u + ADJ_STAGES - 1 < units) issue(u + ADJ_STAGES - 1);
+    if (u + STAGES - 1 < units) issue(u + STAGES - 1);
     cp_async_commit();
-    cp_async_wait<ADJ_STAGES - 1>();
+    cp_async_wait<STAGES - 1>();
     __syncwarp();
-    const uint32_t *svs = sv + (u % ADJ_STAGES) * VSTAGE;
-    const int32_t *scs = sc + (u % ADJ_STAGES) * CSTAGE;
+    const uint32_t *svs = sv + (u % STAGES) * VSTAGE;
+    const uint32_t *scs = sc + (u % STAGES) * CSTAGE;
     float *dp = dvals + o + (size_t)u * S * WS + lane;
-#pragma unroll
-    for (int st = 0; st < S; st++) {
+    auto step = [&](int st) {
       const int q = st * WS + (int)lane;
       const float v = __uint_as_float(svs[q]);
-      const float2 g = WIN ? wp[reinterpret_cast<const uint16_t *>(scs)[q]] : pair_at<float, XD>(xdy, x, dy, scs[q]);
+      float2 g;
+      if constexpr (WIN) {
+        g = wp[reinterpret_cast<const uint16_t *>(scs)[q]];
+      } else {
+        const int c = (int)scs[q];
+        g = make_float2(__ldg(x + c), __ldg(dy + c));
+      }
       acc = fmaf(v, g.y, acc);
       __stcs(dp + st * WS, (int)(u * S + st) < el ? dyr * g.x : 0.f);
+    };
+    if (u < full) {  // a full unit: no guards, so the tile reads can be batched
+#pragma unroll
+      for (int st = 0; st < S; st++) step(st);
+    } else {
+      for (int st = 0; st < (int)rem; st++) step(st);
     }
     __syncwarp();  // this tile is refilled STAGES - 1 units later
   }
   cp_async_wait<0>();
-  __syncwarp();  // the window of a warp without a full unit
-  size_t slot = o + (size_t)units * S * WS + lane;
-  for (uint32_t i = 0; i < rem; i++, slot += WS) {
-    const float2 g = WIN ? wp[ld_col1(w16 + slot, 0, pol)] : pair_at<float, XD>(xdy, x, dy, __ldcs(pc + slot));
-    acc = fmaf(__ldcs(tv + slot), g.y, acc);
-    __stcs(dvals + slot, (int)(units * S + i) < el ? dyr * g.x : 0.f);
-  }
   return acc;
 }
 
-template <bool WIN, bool XD>
-__global__ void __launch_bounds__(ADJ_SW * 32, ADJ_STAGED_BLOCKS) k_adjoint_sym_staged(
+// STAGES tiles in the ring, BLOCKS blocks per SM.  ALLWIN: every warp has
+// an x window, so the column tiles hold 16-bit positions only.
+template <int STAGES, int BLOCKS, bool ALLWIN>
+__global__ void __launch_bounds__(ADJ_SW * 32, BLOCKS) k_adjoint_sym_staged(
     const int4 *__restrict__ desc, uint32_t W, const int32_t *__restrict__ row_map, const uint32_t *__restrict__ slen,
     uint32_t nzr, uint32_t nrows, const int32_t *__restrict__ pc, const uint16_t *__restrict__ w16,
     const int2 *__restrict__ wch, const int4 *__restrict__ wdesc, const float *__restrict__ tv,
-    const float2 *__restrict__ xdy, const float *__restrict__ x, const float *__restrict__ dy, float *__restrict__ dx,
-    float *__restrict__ dvals) {
+    const float *__restrict__ x, const float *__restrict__ dy, float *__restrict__ dx, float *__restrict__ dvals) {
   using namespace core;
   constexpr int S = 8;
-  __shared__ __align__(16) uint32_t s_val[ADJ_SW][ADJ_STAGES * S * WS];
-  __shared__ __align__(16) int32_t s_col[ADJ_SW][ADJ_STAGES * S * WS];
-  __shared__ __align__(16) float2 s_win[WIN ? ADJ_SW : 1][WIN ? WIN_MAX : 1];
+  constexpr int NCW = ALLWIN ? S / 2 : S;  // column words per lane and unit
+  __shared__ __align__(16) uint32_t s_val[ADJ_SW][STAGES * S * WS];
+  __shared__ __align__(16) uint32_t s_col[ADJ_SW][STAGES * NCW * WS];
+  __shared__ __align__(16) float2 s_win[ADJ_SW][WIN_MAX];
   const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x / WS;
   const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
   if (w < W) {
     const uint64_t pol = policy_evict_first();
-    const int4 d = desc[w];
-    const uint32_t T_ = (uint32_t)d.z, A = (uint32_t)d.y, t = lane % T_;
-    const uint32_t p = (uint32_t)d.w + lane / T_;
-    const bool valid = p < nzr;
-    int32_t row = 0;
-    int el = 0;
-    float dyr = 0.f;
-    if (valid) {
-      row = row_map[p];
-      el = max(0, min((int)A, (int)slen[p] - (int)(t * A)));
-      dyr = XD ? dy[row] : xdy[row].y;
+    const int4 d = desc[w], wd = wdesc[w];  // independent loads, in flight together
+    int32_t row;
+    bool valid;
+    float acc;
+    if (ALLWIN || wd.y != 0) {
+      acc = adjoint_warp_pipe<STAGES, true>(d, wd, wch, pc, w16, tv, x, dy, row_map, slen, nzr, s_win[wib], dvals,
+                                            s_val[wib], s_col[wib], lane, pol, row, valid);
+    } else {
+      if constexpr (!ALLWIN)
+        acc = adjoint_warp_pipe<STAGES, false>(d, wd, wch, pc, w16, tv, x, dy, row_map, slen, nzr, nullptr, dvals,
+                                               s_val[wib], s_col[wib], lane, pol, row, valid);
     }
-    const int4 wd = WIN ? wdesc[w] : make_int4(0, 0, 0, 0);
-    const float acc0 =
-        (WIN && wd.y != 0)
-            ? adjoint_warp_pipe<WIN, XD>(d, wd, wch, pc, w16, tv, xdy, x, dy, s_win[wib], dvals, s_val[wib],
-                                         s_col[wib], dyr, el, lane, pol)
-            : adjoint_warp_pipe<false, XD>(d, wd, wch, pc, w16, tv, xdy, x, dy, nullptr, dvals, s_val[wib], s_col[wib],
-                                           dyr, el, lane, pol);
-    float acc = acc0;
+    const uint32_t T_ = (uint32_t)d.z;
     for (uint32_t k = 1; k < T_; k <<= 1) acc += __shfl_down_sync(0xffffffffu, acc, k);
     if (valid && (lane & (T_ - 1)) == 0) dx[row] = acc;
   }
@@ -763,19 +771,16 @@ extern "C" wk_status wk_adjoint_run(wk_adjoint *a, const void *x, const void *dy
         a->win_built = true;
       }
       const unsigned g = (unsigned)std::max<size_t>(1, ((size_t)W + ADJ_SW - 1) / ADJ_SW);
-      if (a->win.warps == W) {  // every warp stages its window: x and dy read directly
-        k_adjoint_sym_staged<true, true><<<g, ADJ_SW * 32, 0, st>>>(
-            L->d.warp_desc, W, L->d.row_map, L->d.slen, L->info.nznrows, n, f->cols.as<int32_t>(),
-            a->win.w16.as<uint16_t>(), a->win.chunks.as<int2>(), a->win.wdesc.as<int4>(), a->te->vals.as<float>(),
-            nullptr, (const float *)x, (const float *)dy, (float *)dx, (float *)dvals);
-      } else {
-        if (a->xdy.bytes < pb) WK_TRY(a->xdy.alloc(pb));
-        k_interleave<float><<<gi, 256, 0, st>>>((const float *)x, (const float *)dy, n, a->xdy.as<float2>());
-        k_adjoint_sym_staged<true, false><<<g, ADJ_SW * 32, 0, st>>>(
-            L->d.warp_desc, W, L->d.row_map, L->d.slen, L->info.nznrows, n, f->cols.as<int32_t>(),
-            a->win.w16.as<uint16_t>(), a->win.chunks.as<int2>(), a->win.wdesc.as<int4>(), a->te->vals.as<float>(),
-            a->xdy.as<float2>(), nullptr, nullptr, (float *)dx, (float *)dvals);
-      }
+#define WK_ADJ_ST(ST, BL, AW)                                                                                      \
+  k_adjoint_sym_staged<ST, BL, AW><<<g, ADJ_SW * 32, 0, st>>>(                                                     \
+      L->d.warp_desc, W, L->d.row_map, L->d.slen, L->info.nznrows, n, f->cols.as<int32_t>(),                      \
+      a->win.w16.as<uint16_t>(), a->win.chunks.as<int2>(), a->win.wdesc.as<int4>(), a->te->vals.as<float>(),      \
+      (const float *)x, (const float *)dy, (float *)dx, (float *)dvals)
+      if (a->win.warps == W)
+        WK_ADJ_ST(4, 5, true);  // 16-bit positions only: 40 KB per block
+      else
+        WK_ADJ_ST(4, 4, false);
+#undef WK_ADJ_ST
       WK_CHECK_LAUNCH();
       return WK_OK;
     }
