@@ -433,22 +433,6 @@ __global__ void __launch_bounds__(AdjCfg<T, CSR>::warps * 32, AdjCfg<T, CSR>::mi
 // measured 0.123-0.129 ms: the second window buffer costs a block per SM.
 constexpr int ADJ_SW = 4;  // warps per block
 
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, uint64_t pol) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(sa), "l"(gmem), "l"(pol)
-               : "memory");
-}
-template <int N>
-__device__ __forceinline__ void cp_async_ca(void *smem, const void *gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(sa), "l"(gmem), "n"(N) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-
 // One layout warp.  Units of S steps; the last unit may be partial (the
 // remainder steps ride in the same ring, copied by the lanes that hold
 // them).  The first STAGES - 1 units are issued as soon as the descriptors

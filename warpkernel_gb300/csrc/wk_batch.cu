@@ -25,6 +25,7 @@ constexpr int WS = 32;
 #define WK_BATCH_BLOCK 256
 #endif
 constexpr int BATCH_BLOCK = WK_BATCH_BLOCK;
+constexpr int BATCH_STAGES = 3;  // tiles in each warp's matrix-stream ring
 
 // X is gathered from a blocked copy: right-hand sides BW*b .. BW*b+BW-1
 // (BW = 16 bytes of T: 4 floats or 2 doubles) of every column form block b,
@@ -68,34 +69,6 @@ __device__ __forceinline__ void set_vec(double (&g)[2], const double2 f) {
   g[0] = f.x; g[1] = f.y;
 }
 
-// g = the TR right-hand sides j0 .. j0+TR-1 of column c (zeros from jn on).
-// xt = the tile's first block plus j0 % BW (Xb + (j0 / BW) * bstride +
-// j0 % BW), bstride = ncols * BW elements; a matrix's blocked X holds fewer
-// than 2^32 elements (wk_batch_set_vectors checks), so offsets fit 32 bits.
-template <typename T, int TR>
-__device__ __forceinline__ void gather_tile(const T *__restrict__ xt, uint32_t c, uint32_t bstride, int jn,
-                                            T (&g)[TR]) {
-  constexpr int BW = Blk<T>::BW;
-  typedef typename Blk<T>::V V;
-  const T *xc = xt + (size_t)c * BW;
-  if constexpr (TR >= BW) {
-#pragma unroll
-    for (int j = 0; j < TR; j += BW) {
-      T q[BW];
-      if (j < jn)
-        set_vec(q, __ldg(reinterpret_cast<const V *>(xc + (uint32_t)(j / BW) * bstride)));
-      else
-#pragma unroll
-        for (int i = 0; i < BW; i++) q[i] = T(0);
-#pragma unroll
-      for (int i = 0; i < BW; i++) g[j + i] = q[i];
-    }
-  } else {  // the tile lies inside one block
-#pragma unroll
-    for (int j = 0; j < TR; j++) g[j] = j < jn ? __ldg(xc + j) : T(0);
-  }
-}
-
 // The blocked copy of X: one block of threads per item, thread i of a row
 // range handles (row r0 + i / nb, block i % nb).
 template <typename T>
@@ -124,11 +97,10 @@ __global__ void __launch_bounds__(256) k_xblock(const XCopy<T> *__restrict__ ite
   }
 }
 
-// Value / column words of one unit of S steps (S slots of 32 B per lane).
+// One unit of the matrix stream: S steps, 32 bytes of values per lane.
 template <typename T>
 struct Unit {
   static constexpr int S = 32 / (int)sizeof(T);  // float: 8 steps, double: 4
-  static constexpr int NWC = S;                   // column words per lane
 };
 
 template <typename T>
@@ -142,29 +114,143 @@ __device__ __forceinline__ double staged_val<double>(const uint32_t *sv, int q) 
   return __hiloint2double((int)sv[2 * q + 1], (int)sv[2 * q]);
 }
 
-// The matrix stream of a layout warp is read a unit of S steps at a time
-// with one 32-byte load of values and one of columns per lane (the same
-// coalesced words lane_sum_vec reads), staged through shared memory in slot
-// order and read back as S consecutive steps of the lane's own layout lane,
-// so each lane keeps one accumulator per right-hand side.  The next unit's
-// loads are issued before the current unit's gathers.  Per lane the steps
-// are summed in order (fma from zero), which is the reference's order.
-// Three resident blocks per SM: uncapped, the 16-RHS float kernel takes 117
-// registers (two blocks, 16 warps per SM); capped at 85 it measured 11 % faster.
-// fp64 with a 16-wide tile (32 registers of accumulators and 32 of gathered
-// X) gets two blocks per SM: capped for three it spilled 336 bytes.
+// Three resident blocks per SM: uncapped, the 16-RHS float kernel takes more
+// than 100 registers (two blocks, 16 warps per SM); capped at 80 it runs
+// with 8 bytes of spill.  fp64 with a 16-wide tile (32 registers of
+// accumulators and 32 of gathered X) gets two blocks per SM.
 template <typename T, int TR>
 constexpr int batch_min_blocks() {
   return sizeof(T) == 8 && TR >= 16 ? 2 : 3;
 }
+// Layout warps [w0, w1) of one matrix for right-hand sides j0 .. j0 + jn - 1
+// with TT accumulators per lane.  TT >= BW: TT / BW whole 16-byte groups
+// per slot, unguarded (the blocked copy is zero past k, and only j < jn is
+// stored; GUARD skips the groups past jn); TT < BW: the tile lies inside one
+// group, gathered element-wise.  The matrix stream of each layout warp runs
+// through a ring of BATCH_STAGES tiles of S steps in shared memory, filled
+// by cp.async two units ahead (the partial last unit included, copied by
+// the lanes that hold its slots) and read back in slot order, so lane l
+// sums its own layout lane's slots in step order (fma from zero), which is
+// the reference's order.  The next layout warp's descriptor is loaded while
+// the current one streams.
+template <typename T, int TT, bool GUARD = false>
+__device__ __forceinline__ void batch_tile(const BatchMat<T> &M, uint32_t w0, uint32_t w1, uint32_t j0, int jn,
+                                           uint32_t *sv, int32_t *sc, uint32_t lane, uint64_t pol) {
+  using namespace core;
+  constexpr int S = Unit<T>::S, BW = Blk<T>::BW, STAGES = BATCH_STAGES;
+  constexpr int LV = S * (int)sizeof(T) / 4;  // value words per lane and unit
+  constexpr int VW = LV * WS, CW = S * WS;    // words per value / column tile
+  typedef typename Blk<T>::V V;
+  const uint32_t bstride = M.ncols * (uint32_t)BW;
+  const T *xt = M.Xb + (size_t)(j0 / BW) * bstride + (j0 % BW);
+  auto gather = [&](uint32_t c, T(&g)[TT]) {
+    const T *xc = xt + (size_t)c * BW;
+    if constexpr (TT >= BW) {
+#pragma unroll
+      for (int j = 0; j < TT; j += BW) {
+        T q[BW];
+        if (!GUARD || j < jn)
+          set_vec(q, __ldg(reinterpret_cast<const V *>(xc + (uint32_t)(j / BW) * bstride)));
+        else
+#pragma unroll
+          for (int i = 0; i < BW; i++) q[i] = T(0);
+#pragma unroll
+        for (int i = 0; i < BW; i++) g[j + i] = q[i];
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < TT; j++) g[j] = j < jn ? __ldg(xc + j) : T(0);
+    }
+  };
+  int4 dn = w0 < w1 ? M.desc[w0] : make_int4(0, 0, 0, 0);
+  for (uint32_t w = w0; w < w1; w++) {
+    const int4 d = dn;
+    if (w + 1 < w1) dn = M.desc[w + 1];
+    const uint32_t T_ = (uint32_t)d.z, A = (uint32_t)d.y;
+    const size_t o = (size_t)(uint32_t)d.x;
+    const uint32_t full = A / S, rem = A % S, units = full + (rem != 0);
+    // unit u: steps [u S, u S + S) of all lanes, S * 32 consecutive slots;
+    // lane l copies slots [S l, S l + S) of it
+    auto issue = [&](uint32_t u) {
+      if (u < full || lane < rem * (WS / S)) {
+        const size_t g = o + (size_t)u * S * WS + S * lane;
+        uint32_t *dv = sv + (u % STAGES) * VW + LV * lane;
+        const uint32_t *gv = reinterpret_cast<const uint32_t *>(M.vals + g);
+#pragma unroll
+        for (int q = 0; q < LV; q += 4) cp_async16(dv + q, gv + q, pol);
+        int32_t *dc = sc + (u % STAGES) * CW + S * lane;
+#pragma unroll
+        for (int q = 0; q < S; q += 4) cp_async16(dc + q, M.cols + g + q, pol);
+      }
+    };
+#pragma unroll
+    for (int s0 = 0; s0 < STAGES - 1; s0++) {
+      if ((uint32_t)s0 < units) issue((uint32_t)s0);
+      cp_async_commit();
+    }
+    const uint32_t p = (uint32_t)d.w + lane / T_;
+    const bool valid = p < M.nzr;
+    const int32_t row = valid ? M.row_map[p] : 0;
+    T acc[TT];
+#pragma unroll
+    for (int j = 0; j < TT; j++) acc[j] = T(0);
+    for (uint32_t u = 0; u < units; u++) {
+      if (u + STAGES - 1 < units) issue(u + STAGES - 1);
+      cp_async_commit();
+      cp_async_wait<STAGES - 1>();
+      __syncwarp();
+      const uint32_t *svs = sv + (u % STAGES) * VW;
+      const int32_t *scs = sc + (u % STAGES) * CW;
+      auto step = [&](int st) {
+        const int q = st * WS + (int)lane;
+        const T v = staged_val<T>(svs, q);
+        T g[TT];
+        gather((uint32_t)scs[q], g);
+#pragma unroll
+        for (int j = 0; j < TT; j++) acc[j] = fma(v, g[j], acc[j]);
+      };
+      if (u < full) {
+#pragma unroll
+        for (int st = 0; st < S; st++) step(st);
+      } else {
+        for (int st = 0; st < (int)rem; st++) step(st);
+      }
+      __syncwarp();  // this tile is refilled STAGES - 1 units later
+    }
+#pragma unroll
+    for (int j = 0; j < TT; j++)
+      for (uint32_t s2 = 1; s2 < T_; s2 <<= 1) acc[j] += __shfl_down_sync(0xffffffffu, acc[j], s2);
+    if (valid && (lane & (T_ - 1)) == 0) {
+      T *yr = M.Y + (size_t)row * M.k + j0;
+#pragma unroll
+      for (int j = 0; j < TT; j++)
+        if (j < jn) __stcs(yr + j, acc[j]);  // streaming: keeps X in L2 (1.5 % faster)
+    }
+  }
+}
+
+// NG = TR / BW 16-byte groups at most; a tile of jn right-hand sides runs
+// the instance with ceil(jn / BW) groups.
+template <typename T, int TR, int G = 1>
+__device__ __forceinline__ void batch_tile_groups(int ng, const BatchMat<T> &M, uint32_t w0, uint32_t w1, uint32_t j0,
+                                                  int jn, uint32_t *sv, int32_t *sc, uint32_t lane, uint64_t pol) {
+  constexpr int BW = Blk<T>::BW;
+  if constexpr (G * BW <= TR) {
+    if (ng == G)
+      batch_tile<T, G * BW, (G * BW == TR)>(M, w0, w1, j0, jn, sv, sc, lane, pol);
+    else
+      batch_tile_groups<T, TR, G + 1>(ng, M, w0, w1, j0, jn, sv, sc, lane, pol);
+  }
+}
+
 template <typename T, int TR>
 __global__ void __launch_bounds__(BATCH_BLOCK, (batch_min_blocks<T, TR>())) k_batch(const BatchMat<T> *__restrict__ mats,
                                                         const int4 *__restrict__ items, uint32_t nitems,
                                                         unsigned *__restrict__ counter) {
-  constexpr int S = Unit<T>::S, NWC = Unit<T>::NWC;
-  constexpr int NSV = S * WS * (int)sizeof(T) / 4;  // staged value words per warp
-  __shared__ __align__(16) uint32_t s_val[BATCH_BLOCK / WS][NSV];
-  __shared__ __align__(16) int32_t s_col[BATCH_BLOCK / WS][S * WS];
+  constexpr int S = Unit<T>::S, BW = Blk<T>::BW;
+  constexpr int NSV = S * WS * (int)sizeof(T) / 4;  // value words per tile
+  __shared__ __align__(16) uint32_t s_val[BATCH_BLOCK / WS][BATCH_STAGES * NSV];
+  __shared__ __align__(16) int32_t s_col[BATCH_BLOCK / WS][BATCH_STAGES * S * WS];
   const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x / WS;
   uint32_t *sv = s_val[wib];
   int32_t *sc = s_col[wib];
@@ -176,69 +262,12 @@ __global__ void __launch_bounds__(BATCH_BLOCK, (batch_min_blocks<T, TR>())) k_ba
     if (it >= nitems) break;
     const int4 item = items[it];
     const BatchMat<T> M = mats[item.x];
-    const uint32_t k = M.k;
-    const uint32_t bstride = M.ncols * (uint32_t)Blk<T>::BW;
-    for (uint32_t w = (uint32_t)item.y; w < (uint32_t)item.z; w++) {
-      const int4 d = M.desc[w];
-      const uint32_t T_ = (uint32_t)d.z, A = (uint32_t)d.y;
-      const uint32_t p = (uint32_t)d.w + lane / T_;
-      const bool valid = p < M.nzr;
-      const size_t o = (size_t)(uint32_t)d.x;
-      const uint32_t units = A / S, rem = A % S;
-      for (uint32_t j0 = 0; j0 < k; j0 += TR) {
-        const int jn = (int)min((uint32_t)TR, k - j0);
-        const T *xt = M.Xb + (size_t)(j0 / Blk<T>::BW) * bstride + (j0 % Blk<T>::BW);
-        T acc[TR];
-#pragma unroll
-        for (int j = 0; j < TR; j++) acc[j] = T(0);
-        uint32_t wv[8], wc[NWC];
-        if (units) {
-          core::ld_words(M.vals + o + S * lane, wv, pol);
-          core::ld_words(M.cols + o + S * lane, wc, pol);
-        }
-        for (uint32_t u = 0; u < units; u++) {
-          __syncwarp();
-#pragma unroll
-          for (int q = 0; q < 8; q += 4)
-            *reinterpret_cast<uint4 *>(sv + 8 * lane + q) = make_uint4(wv[q], wv[q + 1], wv[q + 2], wv[q + 3]);
-#pragma unroll
-          for (int q = 0; q < NWC; q += 4)
-            *reinterpret_cast<uint4 *>(sc + NWC * lane + q) = make_uint4(wc[q], wc[q + 1], wc[q + 2], wc[q + 3]);
-          __syncwarp();
-          if (u + 1 < units) {
-            const size_t nxt = o + (size_t)(u + 1) * S * WS + S * lane;
-            core::ld_words(M.vals + nxt, wv, pol);
-            core::ld_words(M.cols + nxt, wc, pol);
-          }
-#pragma unroll
-          for (int st = 0; st < S; st++) {
-            const int q = st * WS + (int)lane;
-            const T v = staged_val<T>(sv, q);
-            T g[TR];
-            gather_tile<T, TR>(xt, (uint32_t)sc[q], bstride, jn, g);
-#pragma unroll
-            for (int j = 0; j < TR; j++) acc[j] = fma(v, g[j], acc[j]);
-          }
-        }
-        size_t slot = o + (size_t)units * S * WS + lane;
-        for (uint32_t i = 0; i < rem; i++, slot += WS) {
-          const T v = __ldcs(M.vals + slot);
-          const int c = __ldcs(M.cols + slot);
-          T g[TR];
-          gather_tile<T, TR>(xt, (uint32_t)c, bstride, jn, g);
-#pragma unroll
-          for (int j = 0; j < TR; j++) acc[j] = fma(v, g[j], acc[j]);
-        }
-#pragma unroll
-        for (int j = 0; j < TR; j++)
-          for (uint32_t s2 = 1; s2 < T_; s2 <<= 1) acc[j] += __shfl_down_sync(0xffffffffu, acc[j], s2);
-        if (valid && (lane & (T_ - 1)) == 0) {
-          T *yr = M.Y + (size_t)M.row_map[p] * k + j0;
-#pragma unroll
-          for (int j = 0; j < TR; j++)
-            if (j < jn) __stcs(yr + j, acc[j]);  // streaming: keeps X in L2 (1.5 % faster)
-        }
-      }
+    for (uint32_t j0 = 0; j0 < M.k; j0 += TR) {
+      const int jn = (int)min((uint32_t)TR, M.k - j0);
+      if constexpr (TR >= BW)
+        batch_tile_groups<T, TR>((jn + BW - 1) / BW, M, (uint32_t)item.y, (uint32_t)item.z, j0, jn, sv, sc, lane, pol);
+      else
+        batch_tile<T, TR>(M, (uint32_t)item.y, (uint32_t)item.z, j0, jn, sv, sc, lane, pol);
     }
   }
 }

@@ -24,6 +24,26 @@ __device__ __forceinline__ uint64_t policy_evict_first() {
   return pol;
 }
 
+// ---- cp.async: global -> shared copies tracked by commit groups ----------------
+// 16 bytes, L2-only (.cg) with an L2 cache-policy hint; both addresses 16-byte aligned.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, uint64_t pol) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(sa), "l"(gmem), "l"(pol)
+               : "memory");
+}
+// N = 4, 8 or 16 bytes through L1 (.ca); both addresses N-byte aligned.
+template <int N>
+__device__ __forceinline__ void cp_async_ca(void *smem, const void *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(sa), "l"(gmem), "n"(N) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// Waits until at most N of this thread's committed groups are pending.
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 // ---- streaming loads (matrix), ld.global.nc.L1::no_allocate + evict_first ------
 template <typename T>
 __device__ __forceinline__ T ld_stream1(const T *p, uint64_t pol);
