@@ -109,3 +109,26 @@ def test_batch_fp64_and_validation():
     nr = np.zeros(1, np.uint32)
     arr = (C.c_void_p * 1)(b.engines[0].handle.value)
     assert load().wk_batch_create(arr, nr.ctypes.data_as(C.POINTER(C.c_uint32)), 1, 4, 16, C.byref(h)) == 1
+
+
+@pytest.mark.parametrize("dtype", ["f32", "f64"])
+def test_batch_more_rhs_than_the_tile(dtype):
+    """Right-hand-side counts above the widest tile (17-40): each item runs
+    several tiles, the last one narrower (its own 16-byte group count), for
+    every tile width; fp32 and fp64 against the oracle, bit for bit."""
+    import torch
+
+    from warpkernel_gb300 import batched
+    specs = batched.fe_matrix_set(6, seed=13, rows=(400, 4_000))
+    for s, k in zip(specs, (17, 20, 23, 31, 33, 40)):
+        s["nrhs"] = k
+    b = batched.Batch.from_fe(specs, dtype, threshold_frac=1.0, rhs_tile=16, chunk=4)
+    X, Y = batched.make_vectors(specs, torch.float32 if dtype == "f32" else torch.float64)
+    b.set_vectors(X, Y)
+    ref = oracle_products(specs, b, X, dtype)
+    for tile in batched.TILES:
+        b.set_tile(tile)
+        for y in Y:
+            y.zero_()
+        b.run()
+        check(Y, ref, tile)
