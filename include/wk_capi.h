@@ -214,19 +214,21 @@ wk_status wk_engine_destroy(wk_engine *e);
 wk_status wk_engine_compress_cols(wk_engine *e, void *stream, uint32_t *wide_warps);
 
 /* x windows (no reference counterpart; shared-memory staging of x in place of
- * the reference's texture fetch, warpkernel.hpp:27-49), off by default.
- * `on` = 1 (after wk_engine_compress_cols; WK_ERR_STATE otherwise) gives
- * every narrow layout warp with at most 512 distinct columns, in at most 32
- * chunks of <= 32 consecutive columns, an x window: its distinct columns as
- * chunks, and per slot the window position of its column (2 B, a second
- * per-slot array built on the first call).  Fast-order wk_run / wk_run_x then
- * copy each such warp's x values into shared memory, one warp-wide load per
- * chunk, and gather from there instead of from L1/L2; the sums are the same
- * bits.  On GB300 this measured 1-8 % slower than the L1/L2 gathers for the
- * 16-bit-column kernels (hex 96^3: the staging doubles the instructions of a
- * warp's 2,500 slots while the gathers it replaces mostly hit L1), hence off.
- * `on` = 0 switches them off again.  *window_warps (optional) = warps that
- * have a window. */
+ * the reference's texture fetch, warpkernel.hpp:27-49).  With windows on,
+ * wk_engine_compress_cols also gives every narrow layout warp with at most
+ * 512 distinct columns, in at most 32 chunks of <= 32 consecutive columns,
+ * an x window: its distinct columns as chunks, and per slot the window
+ * position of its column (2 B, a second per-slot array).  Fast-order wk_run /
+ * wk_run_x then copy each such warp's x values into shared memory, one
+ * warp-wide copy per chunk, and gather from there instead of from L1/L2; the
+ * sums are the same bits.  On by default for WK_F32 and WK_F16S engines
+ * (4-byte x: the copy is asynchronous and overlaps the first loads of the
+ * matrix stream; hex 96^3 with 16-bit columns, 1-2 % faster than the L1/L2
+ * gathers), off for WK_BF16 (2-byte x is staged by loads and stores before
+ * the stream starts: 9 % slower).  `on` = 1 switches them on (building them
+ * if the compact columns exist; WK_ERR_STATE without them), `on` = 0 off.
+ * *window_warps (optional) = warps that have a window (0 while none are
+ * built). */
 wk_status wk_engine_set_windows(wk_engine *e, int on, uint32_t *window_warps);
 
 /* ---- SpMV --------------------------------------------------------------- */

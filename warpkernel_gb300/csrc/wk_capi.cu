@@ -294,6 +294,10 @@ wk_status wk_engine_create(wk_layout *l, int dtype, const void *vals, const int3
   if (!e) return set_error(WK_ERR_ALLOC, "host allocation failed");
   e->dtype = dtype;
   e->ncols = ncols;
+  // x windows with the compact columns: on for 4-byte x (FP32, scaled FP16),
+  // where the asynchronous window copy made them the faster form; off for
+  // BF16, whose 2-byte x is staged by loads and stores (measured slower)
+  e->use_windows = dtype == WK_F32 || dtype == WK_F16S;
   const size_t anz = l->info.allocate_nz, nz = l->info.nz;
   wk_status s = WK_OK;
   DevView v, c;

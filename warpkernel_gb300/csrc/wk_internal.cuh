@@ -151,7 +151,7 @@ struct wk_engine {
   wk::DevBuf w16, wchunks, wdesc;
   uint32_t window_warps = 0;
   bool windows_built = false;
-  bool use_windows = false;  // wk_engine_set_windows (off by default: measured slower)
+  bool use_windows = false;  // wk_engine_set_windows; wk_engine_create turns it on for FP32 and scaled FP16
   wk::DevBuf scale;  // WK_F16S: float power-of-two scale per layout warp
   // device address of wk_residual_static's static scratch array, looked up
   // on the engine's first wk_residual_static call (an engine lives in one

@@ -117,8 +117,19 @@ __global__ void __launch_bounds__(1024) k_spmv_fast_c(const V *__restrict__ pv, 
   if constexpr (WIN) wd = wdesc[w];
   if (WIN && wd.y != 0) {
     X *win = reinterpret_cast<X *>(wk_dyn_smem) + (threadIdx.x / WS) * WIN_MAX;
-    stage_window<L1>(win, wch, wd, x, lane);
-    s = lane_sum_vec<V, X, L1, uint16_t, true, 0, true>(pv, w16 + (uint32_t)d.x, 0, d, win, lane, pol);
+    // 4-byte x: the window is copied asynchronously and waited for once the
+    // first unit's loads are in flight; 2-byte x (no cp.async of that size)
+    // is staged by the warp's loads and stores first
+    if constexpr (sizeof(X) == 4) {
+      stage_window_async(win, wch, wd, x, lane);
+      s = lane_sum_vec<V, X, L1, uint16_t, true, 0, true>(pv, w16 + (uint32_t)d.x, 0, d, win, lane, pol, [] {
+        cp_async_wait<0>();
+        __syncwarp();
+      });
+    } else {  // staged in four-chunk rounds once the first loads were out: 0.179 ms against 0.158 (bf16, hex 96^3)
+      stage_window<L1>(win, wch, wd, x, lane);
+      s = lane_sum_vec<V, X, L1, uint16_t, true, 0, true>(pv, w16 + (uint32_t)d.x, 0, d, win, lane, pol);
+    }
   } else {
     s = lane_sum_compressed<V, X, L1>(pv, c16, c32, d, cdesc[w], x, lane, pol);
   }

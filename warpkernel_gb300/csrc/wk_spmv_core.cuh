@@ -168,6 +168,25 @@ __device__ __forceinline__ void stage_window(X *win, const int2 *__restrict__ ch
   __syncwarp();
 }
 
+// The same copy for 4-byte x by cp.async, one warp-wide copy per chunk in a
+// rolled loop, committed as one group: the caller issues its first stream
+// loads and then waits (cp_async_wait<0> + __syncwarp) before the first
+// gather, so the window's L2 round trip overlaps the stream's.
+template <typename X>
+__device__ __forceinline__ void stage_window_async(X *win, const int2 *__restrict__ chunks, int4 wd,
+                                                   const X *__restrict__ x, uint32_t lane) {
+  static_assert(sizeof(X) == 4, "cp.async copies 4-byte x values");
+  const int nch = wd.y;
+  const int2 mine = lane < (uint32_t)nch ? chunks[wd.x + lane] : make_int2(0, 0);
+  for (int q = 0; q < nch; q++) {
+    const int c0 = __shfl_sync(0xffffffffu, mine.x, q);
+    const int pl = __shfl_sync(0xffffffffu, mine.y, q);
+    const int pos = (pl & 0xffff) + (int)lane;
+    if (lane < (uint32_t)(pl >> 16) && pos < WIN_MAX) cp_async_ca<4>(win + pos, x + c0 + (int)lane);
+  }
+  cp_async_commit();
+}
+
 __device__ __forceinline__ double fma_acc(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float fma_acc(float a, float b, float c) { return fmaf(a, b, c); }
 
@@ -370,10 +389,14 @@ __device__ __forceinline__ T block_sum_staged(T v, T *sh) {
 // offsets.
 // UNR (if non-zero) replaces the plan's unroll factor.  SX: x is the warp's
 // x window in shared memory and the columns are window positions (base 0).
-template <typename V, typename X, bool L1, typename C, bool TUNED = true, int UNR = 0, bool SX = false>
+struct NoHook {
+  __device__ __forceinline__ void operator()() const {}
+};
+template <typename V, typename X, bool L1, typename C, bool TUNED = true, int UNR = 0, bool SX = false,
+          typename Hook = NoHook>
 __device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict__ pv, const C *__restrict__ cp0, int base,
                                                            int4 d, const X *__restrict__ x, uint32_t lane,
-                                                           uint64_t pol) {
+                                                           uint64_t pol, Hook hook = Hook()) {
   typedef typename Tr<V>::Acc Acc;
   typedef typename std::conditional<TUNED, VecPlan<V, C>, PlainPlan<V, C>>::type Plan;
   constexpr int S = Plan::slots;
@@ -416,6 +439,7 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict_
     uint32_t wv[NWV], wc[NWC];
     ld_words(vp, wv, pol);
     ld_words(cp, wc, pol);
+    if (u == 0) hook();  // e.g. completing the x window, once the first unit's loads are in flight
 #pragma unroll
     for (int k = 0; k < S; k++)
       a[k] = fma_acc(Tr<V>::acc(word_val<V>(wv, k)), (Acc)Tr<X>::acc(gx<L1, SX>(x, word_col<C>(wc, k, base))), a[k]);
@@ -430,6 +454,7 @@ __device__ __forceinline__ typename Tr<V>::Acc lane_sum_vec(const V *__restrict_
   // made layouts of long warps 15 % slower; with 8 slots the 14 preloaded
   // registers made scaled FP16 with 16-bit columns (then on 8 slots) 10 %
   // slower.
+  if (units == 0) hook();
   const size_t ut = (size_t)units * S * WS + lane;
   if constexpr (S <= 4) {
     Acc tv[S - 1], tx[S - 1];

@@ -356,7 +356,8 @@ class engine:
 
     def set_windows(self, on=True):
         """x windows of the compact column storage on or off (fast order; the
-        same bits either way); returns the number of warps that have one."""
+        same bits either way; on by default for f32 and f16s engines, built by
+        compress_cols); returns the number of warps that have one."""
         n = C.c_uint32(0)
         check(load().wk_engine_set_windows(self.handle, int(bool(on)), C.byref(n)))
         return int(n.value)
