@@ -580,7 +580,7 @@ wk_status wk_fe_size(int dim, int ex, int ey, int ez, int dof, int64_t *nrows, i
 
 wk_status wk_fe_fill(int dim, int ex, int ey, int ez, int dof, int value_mode, uint64_t seed, int32_t *rowptr,
                      int32_t *cols, double *vals, void *stream) {
-  int64_t n, z;
+  int64_t n = 0, z = 0;
   WK_TRY(wk_fe_size(dim, ex, ey, ez, dof, &n, &z));
   if (z > 0x7fffffffLL) return set_error(WK_ERR_OVERFLOW, "nnz %lld exceeds INT32_MAX", (long long)z);
   if (value_mode != 0 && value_mode != 1) return set_error(WK_ERR_INVALID, "value_mode %d", value_mode);

@@ -252,7 +252,7 @@ wk_status launch_shape(uint32_t W, int nblocks, int blocksize, unsigned *grid, u
 
 wk_status launch_spmv(const RunArgs &a) {
   const wk_layout *l = a.e->layout;
-  unsigned grid, block;
+  unsigned grid = 0, block = 0;
   WK_TRY(launch_shape(l->info.nwarps, a.nblocks, a.blocksize, &grid, &block));
   if (l->info.nwarps == 0) return WK_OK;
   switch (a.e->dtype) {
