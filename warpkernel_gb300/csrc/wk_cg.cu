@@ -2,12 +2,16 @@
 // outer loop, fp32 inner CG on an FP32 / BF16 / scaled-FP16 engine, its dot
 // products summed in FP64 unless the caller asks for FP32) on the WPK layout.
 //
-// All scalars stay on the device.  Each reduction writes block partials that
-// a one-block kernel sums in a fixed order into a slot of `scal`, so results
-// are bit-reproducible.  The kernel that finishes r.r also sets a done flag
-// (converged, or the iteration limit reached); every CG kernel returns at
-// once when the flag is set.  A batch of iterations is captured once in a
-// CUDA graph and replayed; the host reads the flag after each batch.
+// All scalars stay on the device, and every reduction is summed in a fixed
+// order, so results are bit-reproducible.  An iteration is three kernels:
+// the SpMV-dot (q = A p, block partials of p.q, each group of 64 blocks
+// summed by its last block to finish), the vector update (every block sums
+// the group sums for alpha; block partials of r.r) and the p update (every
+// block sums those partials for beta; block 0 stores r.r, counts the
+// iteration and sets the done flag: converged, or the iteration limit
+// reached).  Every CG kernel returns at once when the flag is set.  A batch
+// of iterations is captured once in a CUDA graph and replayed; the host
+// reads the flag after each batch.
 #include <algorithm>
 #include <cmath>
 
@@ -33,6 +37,18 @@ unsigned spmv_dot_grid(const wk_layout *l) {
 size_t cg_partials(const wk_layout *l, unsigned residual_blocks) {
   return std::max<size_t>({residual_blocks, VEC_GRID, spmv_dot_grid(l)});
 }
+// The SpMV-dot's block partials are summed in groups of DOT_GROUP blocks by
+// the last block of each group to finish (a counter per group); the vector
+// update then sums the group sums.  Both orders are fixed.
+constexpr unsigned DOT_GROUP = 64;
+unsigned dot_groups(const wk_layout *l) { return (spmv_dot_grid(l) + DOT_GROUP - 1) / DOT_GROUP; }
+
+// Scratch of one CG run: block partials, the SpMV-dot's group sums and their
+// arrival counters (zero between iterations).
+struct CgScratch {
+  double *partials, *gsum;
+  unsigned *gcnt;
+};
 
 // slots of `scal`
 enum { S_RHO0, S_RHO1, S_PQ, S_BB, S_RR64, S_TOL2, S_DONE, S_ITERS, S_MAXIT, S_COUNT };
@@ -66,9 +82,11 @@ __global__ void __launch_bounds__(CG_BLOCK) k_spmv_dot(const V *__restrict__ pv,
                                                        uint32_t W, const int32_t *__restrict__ row_map, uint32_t nzr,
                                                        uint32_t nrows, const X *__restrict__ p, X *__restrict__ q,
                                                        const double *__restrict__ scal, double *__restrict__ partials,
+                                                       double *__restrict__ gsum, unsigned *__restrict__ gcnt,
                                                        const float *__restrict__ wscale) {
   if (done(scal)) return;
   __shared__ double sh[CG_BLOCK];
+  __shared__ bool s_last;
   const uint32_t lane = threadIdx.x & 31;
   // p . q in FP64 (fp64 vectors, or D64), else in FP32 for the inner solve
   // (then no float <-> double conversions per row on GB300's FP64 pipe)
@@ -100,33 +118,41 @@ __global__ void __launch_bounds__(CG_BLOCK) k_spmv_dot(const V *__restrict__ pv,
        k += (size_t)gridDim.x * blockDim.x)
     q[row_map[k]] = X(0);
   const D t = block_sum_staged<CG_BLOCK, D>(part, reinterpret_cast<D *>(sh));
-  if (threadIdx.x == 0) partials[blockIdx.x] = (double)t;
-}
-
-// scal[out] = fixed-order sum of partials[0..n); with CHECK also counts the
-// iteration and sets the done flag (1: r.r <= tol2, 2: iteration limit).
-template <bool CHECK>
-__global__ void __launch_bounds__(1024) k_finish(const double *__restrict__ partials, unsigned n, double *scal,
-                                                 int out) {
-  if (done(scal)) return;
-  __shared__ double sh[32];
-  double v = 0.0;
-  for (unsigned i = threadIdx.x; i < n; i += blockDim.x) v += partials[i];
-  const double t = block_sum(v, sh);
+  // the last block of each group of DOT_GROUP sums the group's partials
+  const unsigned grp = blockIdx.x / DOT_GROUP;
+  const unsigned gsize = min(DOT_GROUP, gridDim.x - grp * DOT_GROUP);
   if (threadIdx.x == 0) {
-    scal[out] = t;
-    if (CHECK) {
-      const double it = scal[S_ITERS] + 1.0;
-      scal[S_ITERS] = it;
-      if (t <= scal[S_TOL2])
-        scal[S_DONE] = 1.0;
-      else if (it >= scal[S_MAXIT])
-        scal[S_DONE] = 2.0;
+    partials[blockIdx.x] = (double)t;
+    __threadfence();
+    s_last = atomicAdd(&gcnt[grp], 1u) == gsize - 1;
+  }
+  __syncthreads();
+  if (s_last && threadIdx.x < WS) {
+    __threadfence();
+    const uint32_t lane = threadIdx.x;
+    const double *gp = partials + (size_t)grp * DOT_GROUP;
+    double a = (lane < gsize ? __ldcg(gp + lane) : 0.0) + (lane + WS < gsize ? __ldcg(gp + lane + WS) : 0.0);
+#pragma unroll
+    for (int off = 16; off; off >>= 1) a += __shfl_xor_sync(0xffffffffu, a, off);
+    if (lane == 0) {
+      gsum[grp] = a;
+      gcnt[grp] = 0u;  // ready for the next iteration
     }
   }
 }
 
-// x += alpha p, r -= alpha q, partials of r . r; alpha = scal[rho] / scal[pq].
+// Fixed-order sum of v[0..n) by one warp (lane-strided partials, then the
+// xor tree); every lane gets the total.
+__device__ __forceinline__ double warp_sum_array(const double *__restrict__ v, unsigned n, uint32_t lane) {
+  double a = 0.0;
+  for (unsigned i = lane; i < n; i += WS) a += __ldcg(v + i);
+#pragma unroll
+  for (int off = 16; off; off >>= 1) a += __shfl_xor_sync(0xffffffffu, a, off);
+  return a;
+}
+
+// x += alpha p, r -= alpha q, partials of r . r; alpha = scal[rho] / (p . q),
+// p . q summed by every block from the SpMV-dot's group sums.
 // FP32 vectors (the inner solve of IR-CG, whose tolerance is loose) are
 // updated in FP32 arithmetic: on GB300 the float <-> double conversions of an
 // FP64 update run at the FP64 rate and made these vector kernels FP64-bound.
@@ -135,10 +161,17 @@ __global__ void __launch_bounds__(1024) k_finish(const double *__restrict__ part
 template <typename T, bool D64>
 __global__ void __launch_bounds__(VEC_BLOCK) k_update(T *__restrict__ x, T *__restrict__ r, const T *__restrict__ p,
                                                       const T *__restrict__ q, uint32_t n, const double *__restrict__ scal,
-                                                      int i_rho, double *__restrict__ partials) {
+                                                      int i_rho, const double *__restrict__ gsum, unsigned ngroups,
+                                                      double *__restrict__ partials) {
   if (done(scal)) return;
   __shared__ double sh[VEC_BLOCK];
-  const double alpha = safe_div(scal[i_rho], scal[S_PQ]);
+  __shared__ double s_alpha;
+  if (threadIdx.x < WS) {
+    const double pq = warp_sum_array(gsum, ngroups, threadIdx.x);
+    if (threadIdx.x == 0) s_alpha = safe_div(scal[i_rho], pq);
+  }
+  __syncthreads();
+  const double alpha = s_alpha;
   double part = 0.0;
   if constexpr (sizeof(T) == 8) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
@@ -167,12 +200,32 @@ __global__ void __launch_bounds__(VEC_BLOCK) k_update(T *__restrict__ x, T *__re
   if (threadIdx.x == 0) partials[blockIdx.x] = t;
 }
 
-// p = r + beta p, beta = scal[rr] / scal[rho]
+// p = r + beta p, beta = r.r / scal[rho], r.r summed by every block from
+// k_update's partials; block 0 stores it in scal[rr], counts the iteration
+// and sets the done flag (1: r.r <= tol2, 2: iteration limit).
 template <typename T>
 __global__ void __launch_bounds__(VEC_BLOCK) k_pupdate(T *__restrict__ p, const T *__restrict__ r, uint32_t n,
-                                                       const double *__restrict__ scal, int i_rr, int i_rho) {
+                                                       double *scal, int i_rr, int i_rho,
+                                                       const double *__restrict__ partials, unsigned nparts) {
   if (done(scal)) return;
-  const double beta = safe_div(scal[i_rr], scal[i_rho]);
+  __shared__ double s_beta;
+  if (threadIdx.x < WS) {
+    const double rr = warp_sum_array(partials, nparts, threadIdx.x);
+    if (threadIdx.x == 0) {
+      s_beta = safe_div(rr, scal[i_rho]);
+      if (blockIdx.x == 0) {
+        scal[i_rr] = rr;
+        const double it = scal[S_ITERS] + 1.0;
+        scal[S_ITERS] = it;
+        if (rr <= scal[S_TOL2])
+          scal[S_DONE] = 1.0;
+        else if (it >= scal[S_MAXIT])
+          scal[S_DONE] = 2.0;
+      }
+    }
+  }
+  __syncthreads();
+  const double beta = s_beta;
   const T b = (T)beta;  // FP32 vectors: FP32 arithmetic (see k_update)
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     p[i] = r[i] + b * p[i];
@@ -236,7 +289,7 @@ struct CgVectors {
 // One CG iteration; `parity` selects which rho slot is current.  d64: the
 // dot products p . q and r . r of FP32 vectors summed in FP64.
 template <typename X>
-void cg_iteration(const wk_engine *e, const CgVectors<X> &v, double *scal, double *partials, int parity, bool d64,
+void cg_iteration(const wk_engine *e, const CgVectors<X> &v, double *scal, const CgScratch &sc, int parity, bool d64,
                   cudaStream_t st) {
   const wk_layout *l = e->layout;
   const uint32_t W = l->info.nwarps, n = l->info.nrows;
@@ -246,8 +299,8 @@ void cg_iteration(const wk_engine *e, const CgVectors<X> &v, double *scal, doubl
 #define WK_SPMV_DOT2(V, M, D)                                                                                       \
   k_spmv_dot<V, X, M, D><<<g, CG_BLOCK, 0, st>>>(e->vals.as<V>(), e->cols.as<int32_t>(), e->c16.as<uint16_t>(),      \
                                                  e->c32.as<int32_t>(), e->cdesc.as<int4>(), l->d.warp_desc, W,        \
-                                                 l->d.row_map, l->info.nznrows, n, v.p, v.q, scal, partials,       \
-                                                 e->scale.as<float>())
+                                                 l->d.row_map, l->info.nznrows, n, v.p, v.q, scal, sc.partials,    \
+                                                 sc.gsum, sc.gcnt, e->scale.as<float>())
 #define WK_SPMV_DOT1(V, M)                                                                                          \
   do {                                                                                                              \
     if (d64) WK_SPMV_DOT2(V, M, true); else WK_SPMV_DOT2(V, M, false);                                              \
@@ -269,13 +322,12 @@ void cg_iteration(const wk_engine *e, const CgVectors<X> &v, double *scal, doubl
 #undef WK_SPMV_DOT
 #undef WK_SPMV_DOT1
 #undef WK_SPMV_DOT2
-  k_finish<false><<<1, 1024, 0, st>>>(partials, g, scal, S_PQ);
+  const unsigned ng = (g + DOT_GROUP - 1) / DOT_GROUP;
   if (d64)
-    k_update<X, true><<<VEC_GRID, VEC_BLOCK, 0, st>>>(v.x, v.r, v.p, v.q, n, scal, i_rho, partials);
+    k_update<X, true><<<VEC_GRID, VEC_BLOCK, 0, st>>>(v.x, v.r, v.p, v.q, n, scal, i_rho, sc.gsum, ng, sc.partials);
   else
-    k_update<X, false><<<VEC_GRID, VEC_BLOCK, 0, st>>>(v.x, v.r, v.p, v.q, n, scal, i_rho, partials);
-  k_finish<true><<<1, 1024, 0, st>>>(partials, VEC_GRID, scal, i_next);
-  k_pupdate<X><<<VEC_GRID, VEC_BLOCK, 0, st>>>(v.p, v.r, n, scal, i_next, i_rho);
+    k_update<X, false><<<VEC_GRID, VEC_BLOCK, 0, st>>>(v.x, v.r, v.p, v.q, n, scal, i_rho, sc.gsum, ng, sc.partials);
+  k_pupdate<X><<<VEC_GRID, VEC_BLOCK, 0, st>>>(v.p, v.r, n, scal, i_next, i_rho, sc.partials, VEC_GRID);
 }
 
 template <typename X>
@@ -298,10 +350,10 @@ struct IterGraph {
     if (cap) cudaStreamDestroy(cap);
   }
   template <typename X>
-  wk_status build(const wk_engine *e, const CgVectors<X> &v, double *scal, double *partials, int iters, bool d64) {
+  wk_status build(const wk_engine *e, const CgVectors<X> &v, double *scal, const CgScratch &sc, int iters, bool d64) {
     WK_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     WK_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-    for (int i = 0; i < iters; i++) cg_iteration<X>(e, v, scal, partials, i & 1, d64, cap);
+    for (int i = 0; i < iters; i++) cg_iteration<X>(e, v, scal, sc, i & 1, d64, cap);
     cudaGraph_t g = nullptr;
     cudaError_t err = cudaStreamEndCapture(cap, &g);
     if (err != cudaSuccess) {
@@ -360,10 +412,15 @@ extern "C" wk_status wk_cg(wk_engine *e, const double *b, double *x, wk_cg_param
   WK_TRY(qb.alloc((size_t)n * 8));
   WK_TRY(sb.alloc(S_COUNT * 8));
   WK_TRY(part.alloc(cg_partials(e->layout, rg) * 8));
+  DevBuf gs, gc;
+  WK_TRY(gs.alloc((size_t)dot_groups(e->layout) * 8));
+  WK_TRY(gc.alloc((size_t)dot_groups(e->layout) * 4));
+  WK_CUDA(cudaMemsetAsync(gc.p, 0, (size_t)dot_groups(e->layout) * 4, st));
   double *scal = sb.as<double>(), *pp = part.as<double>();
+  const CgScratch sc{pp, gs.as<double>(), gc.as<unsigned>()};
   CgVectors<double> v{x, rb.as<double>(), pb.as<double>(), qb.as<double>()};
   IterGraph gr;
-  WK_TRY(gr.build<double>(e, v, scal, pp, batch_of(prm), true));
+  WK_TRY(gr.build<double>(e, v, scal, sc, batch_of(prm), true));
   cudaEvent_t t0, t1;
   WK_CUDA(cudaEventCreate(&t0));
   WK_CUDA(cudaEventCreate(&t1));
@@ -419,11 +476,16 @@ extern "C" wk_status wk_ir_cg(wk_engine *e64, wk_engine *lo, const double *b, do
   WK_TRY(qb.alloc((size_t)n * 4));
   WK_TRY(sb.alloc(S_COUNT * 8));
   WK_TRY(part.alloc(std::max(cg_partials(lo->layout, rg), cg_partials(e64->layout, rg)) * 8));
+  DevBuf gs, gc;
+  WK_TRY(gs.alloc((size_t)dot_groups(lo->layout) * 8));
+  WK_TRY(gc.alloc((size_t)dot_groups(lo->layout) * 4));
+  WK_CUDA(cudaMemsetAsync(gc.p, 0, (size_t)dot_groups(lo->layout) * 4, st));
   double *r64 = r64b.as<double>(), *scal = sb.as<double>(), *pp = part.as<double>();
+  const CgScratch sc{pp, gs.as<double>(), gc.as<unsigned>()};
   CgVectors<float> v{db.as<float>(), r32b.as<float>(), pb.as<float>(), qb.as<float>()};
   const bool d64 = prm->inner_dots_fp32 == 0;
   IterGraph gr;
-  WK_TRY(gr.build<float>(lo, v, scal, pp, batch_of(prm), d64));
+  WK_TRY(gr.build<float>(lo, v, scal, sc, batch_of(prm), d64));
   cudaEvent_t t0, t1;
   WK_CUDA(cudaEventCreate(&t0));
   WK_CUDA(cudaEventCreate(&t1));
