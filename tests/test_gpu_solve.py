@@ -121,3 +121,36 @@ def test_cg_reports_non_convergence():
     x = torch.zeros(n, dtype=torch.float64, device="cuda")
     res = wk.wpk.cg(eng, b, x, tol=1e-14, max_iter=3, check_every=1)
     assert not res["converged"] and res["iters"] == 3 and res["relres"] > 1e-14
+
+
+def test_cg_and_ir_cg_repeat_bit_for_bit_across_partial_groups():
+    """hex 14^3 x 3 dof (10,125 rows, 317 layout warps): the SpMV-dot's 80
+    blocks form one full group of 64 and a partial one, whose sums are made
+    by whichever block arrives last.  Two solves give the same iterations and
+    the same bits (fp64 CG and IR-CG with an FP32 inner solve), and they
+    reach the tolerance against the host CSR product."""
+    import torch
+
+    import warpkernel_gb300 as wk
+    rp, cols, vals = O.fe_matrix(3, 14, 14, 14, 3, value_mode=1, seed=6)
+    n = len(rp) - 1
+    b = O.csr_spmv(rp, cols, vals, O.uniform_vec(5, 0, n))
+    db = torch.from_numpy(b).cuda()
+    k, e64 = setup(rp, cols, vals, 2, 81)
+    assert k.nwarps > 4 * 64
+    lo = wk.engine(k, wk.fe.convert(torch.from_numpy(vals).cuda(), torch.float32), torch.from_numpy(cols).cuda(),
+                   dtype="f32")
+    lo.compress_cols()
+    for solve in (lambda x: wk.wpk.cg(e64, db, x, tol=1e-10),
+                  lambda x: wk.wpk.ir_cg(e64, lo, db, x, tol=1e-10, inner_tol=1e-4)):
+        xs, its = [], []
+        for _ in range(2):
+            x = torch.zeros(n, dtype=torch.float64, device="cuda")
+            res = solve(x)
+            assert res["converged"], res
+            xs.append(x.cpu().numpy())
+            its.append((res["iters"], res["outer"]))
+        assert its[0] == its[1]
+        assert np.array_equal(xs[0].view(np.uint64), xs[1].view(np.uint64))
+        r = b - O.csr_spmv(rp, cols, vals, xs[0])
+        assert np.linalg.norm(r) / np.linalg.norm(b) <= 1.1e-10
