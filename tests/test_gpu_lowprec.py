@@ -239,3 +239,72 @@ def test_x_windows_give_the_same_bits(dtype):
                         (eng.run if mapped else eng.run_x)(0, bs, x, y, order=0)
                         out[on] = y
                     assert t.equal(out[True], out[False]), (name, dtype, kind, bs, mapped)
+
+
+def _window_case_sets():
+    """Per layout warp: (sorted distinct columns relative to the warp's base,
+    whether the warp gets an x window: at most 512 distinct columns in at
+    most 32 runs, at most 32 chunks of <= 32 consecutive columns, and a
+    span below 65,536)."""
+    def runs(starts, length):
+        return [s + i for s in starts for i in range(length)]
+    cases = [
+        (runs(range(0, 16 * 37, 37), 32), True),                               # 512 distinct, 16 chunks
+        (runs(range(0, 16 * 37, 37), 32) + [16 * 37 + 5], False),              # 513 distinct
+        (runs(range(0, 32 * 5, 5), 3), True),                                  # 32 runs, 32 chunks
+        (runs(range(0, 33 * 5, 5), 3), False),                                 # 33 runs
+        (runs(range(30, 30 + 12 * 47, 47), 40), True),                         # 2 chunks per run, 24 chunks;
+                                                                               # runs cross bitmap words
+        (runs(range(0, 7 * 70, 70), 65), True),                                # 3 chunks per run, 21 chunks
+        (runs(range(0, 15 * 40, 40), 33) + [700, 710, 720], False),            # 33 chunks, 498 distinct
+        (runs(range(0, 17 * 19, 19), 17), True),                               # odd run lengths
+        (runs([0, 65535 - 31], 32), True),                                     # span 65,535
+        (runs([0, 70000], 32), False),                                         # span above 65,535: 32-bit
+    ]
+    return cases
+
+
+@pytest.mark.parametrize("dtype", ["f32", "f16s"])
+def test_x_window_limits(dtype):
+    """Warps built to sit on every limit of the x windows (distinct columns,
+    runs, chunks after splitting runs longer than 32, bitmap word crossings,
+    the 16-bit span): exactly the eligible warps get a window, and run /
+    run_x give the same bits with the windows on and off, against the
+    oracle's FP32 restatement within 1e-6."""
+    t = _t()
+    wk = _wk()
+    rng = np.random.default_rng(21)
+    cases = _window_case_sets()
+    L, base_step = 32, 140_000
+    rows, colsl = [], []
+    for j, (cset, _) in enumerate(cases):
+        S = len(cset)
+        for i in range(32):
+            idx = [(i * L + q) % S for q in range(L)]
+            colsl.append(sorted(j * base_step + cset[q] for q in idx))
+    n, ncols = len(colsl), len(cases) * base_step
+    rp = np.arange(n + 1, dtype=np.int32) * L
+    cols = np.concatenate(colsl).astype(np.int32)
+    vals = rng.uniform(-1, 1, len(cols))
+    x = rng.uniform(-1, 1, ncols)
+    k = wk.structure()
+    k.scan(len(cols), n, None, rp, None)
+    assert k.nwarps == len(cases)
+    eng = wk.engine(k, wk.fe.convert(t.from_numpy(vals).cuda(), t.float32), t.from_numpy(cols).cuda(), dtype=dtype,
+                    ncols=ncols)
+    wide = eng.compress_cols()
+    assert wide == 1
+    assert eng.set_windows(True) == sum(ok for _, ok in cases)
+    xd = t.from_numpy(x).cuda().float()
+    y_ref = O.csr_spmv(rp, cols, vals, x)
+    for mapped in (True, False):
+        out = {}
+        for on in (True, False):
+            eng.set_windows(on)
+            y = t.zeros(n, dtype=t.float32, device="cuda")
+            (eng.run if mapped else eng.run_x)(0, 128, xd, y, order=0)
+            out[on] = y
+        assert t.equal(out[True], out[False]), (dtype, mapped)
+    yh = out[True].double().cpu().numpy()
+    tol = REL_TOL_F32_VS_F64 if dtype == "f32" else 1e-3
+    assert np.linalg.norm(yh - y_ref) / np.linalg.norm(y_ref) < tol
