@@ -421,8 +421,8 @@ enum {
 /* dx = A^T dy (ncols entries; NULL to skip) and dvals = dy[row(k)] x[col(k)]
  * for every stored entry k (NULL to skip), in `dvals_order`.  x, dy, dx,
  * dvals are device vectors of fwd's dtype.  WK_DVALS_SLOTS writes the
- * gradient where the values are stored, with coalesced vector stores (the
- * fastest form).  Stream-ordered. */
+ * gradient where the values are stored, with coalesced stores (the fastest
+ * form; dvals 32-byte aligned).  Stream-ordered. */
 wk_status wk_adjoint_run(wk_adjoint *a, const void *x, const void *dy, void *dx, void *dvals,
                          int dvals_order, void *stream);
 
