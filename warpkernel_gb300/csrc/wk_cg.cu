@@ -73,7 +73,9 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
 
 // q = A p (rows without entries get 0) and block partials of p . q.  MODE 0:
 // vector path, 1: vector path on 16-bit columns, 2: one slot per step (short
-// warps, as wk_run's fast order chooses).  D64: p . q accumulated in FP64
+// warps, as wk_run's fast order chooses), 3: 16-bit columns with the
+// engine's x windows (4-byte vectors; dynamic shared memory of WIN_MAX
+// values per warp), the window copied asynchronously as in wk_run.  D64: p . q accumulated in FP64
 // (each row's p and q converted once), else in the vectors' precision.
 template <typename V, typename X, int MODE, bool D64>
 __global__ void __launch_bounds__(CG_BLOCK) k_spmv_dot(const V *__restrict__ pv, const int32_t *__restrict__ pc,
@@ -83,8 +85,10 @@ __global__ void __launch_bounds__(CG_BLOCK) k_spmv_dot(const V *__restrict__ pv,
                                                        uint32_t nrows, const X *__restrict__ p, X *__restrict__ q,
                                                        const double *__restrict__ scal, double *__restrict__ partials,
                                                        double *__restrict__ gsum, unsigned *__restrict__ gcnt,
-                                                       const float *__restrict__ wscale) {
+                                                       const float *__restrict__ wscale, const uint16_t *__restrict__ w16,
+                                                       const int2 *__restrict__ wch, const int4 *__restrict__ wdesc) {
   if (done(scal)) return;
+  extern __shared__ __align__(16) unsigned char cg_dyn_smem[];
   __shared__ double sh[CG_BLOCK];
   __shared__ bool s_last;
   const uint32_t lane = threadIdx.x & 31;
@@ -99,7 +103,19 @@ __global__ void __launch_bounds__(CG_BLOCK) k_spmv_dot(const V *__restrict__ pv,
     const uint32_t T = (uint32_t)d.z;
     const uint32_t r = (uint32_t)d.w + lane / T;
     typename Tr<V>::Acc s;
-    if constexpr (MODE == 1)
+    if constexpr (MODE == 3 && sizeof(X) == 4) {
+      const int4 wd = wdesc[w];
+      if (wd.y != 0) {
+        X *win = reinterpret_cast<X *>(cg_dyn_smem) + (threadIdx.x / WS) * WIN_MAX;
+        stage_window_async(win, wch, wd, p, lane);
+        s = lane_sum_vec<V, X, true, uint16_t, false, 0, true>(pv, w16 + (uint32_t)d.x, 0, d, win, lane, pol, [] {
+          cp_async_wait<0>();
+          __syncwarp();
+        });
+      } else {
+        s = lane_sum_compressed<V, X, true, false>(pv, c16, c32, d, cdesc[w], p, lane, pol);
+      }
+    } else if constexpr (MODE == 1 || MODE == 3)
       s = lane_sum_compressed<V, X, true, false>(pv, c16, c32, d, cdesc[w], p, lane, pol);
     else if constexpr (MODE == 2)
       s = lane_sum_exact<V, X, true>(pv, pc, d, p, lane, r < nzr);
@@ -295,19 +311,24 @@ void cg_iteration(const wk_engine *e, const CgVectors<X> &v, double *scal, const
   const uint32_t W = l->info.nwarps, n = l->info.nrows;
   const unsigned g = spmv_dot_grid(l);
   const int i_rho = parity ? S_RHO1 : S_RHO0, i_next = parity ? S_RHO0 : S_RHO1;
-  const int mode = short_layout(l, e->dtype) ? 2 : (e->compressed && e->dtype != WK_F64 ? 1 : 0);
+  int mode = short_layout(l, e->dtype) ? 2 : (e->compressed && e->dtype != WK_F64 ? 1 : 0);
+  // the engine's x windows for 4-byte vectors (FP32 and scaled-FP16 engines)
+  if (mode == 1 && sizeof(X) == 4 && e->dtype != WK_BF16 && e->use_windows && e->windows_built && e->window_warps)
+    mode = 3;
+  const size_t smem = mode == 3 ? (size_t)(CG_BLOCK / WS) * WIN_MAX * sizeof(X) : 0;
 #define WK_SPMV_DOT2(V, M, D)                                                                                       \
-  k_spmv_dot<V, X, M, D><<<g, CG_BLOCK, 0, st>>>(e->vals.as<V>(), e->cols.as<int32_t>(), e->c16.as<uint16_t>(),      \
-                                                 e->c32.as<int32_t>(), e->cdesc.as<int4>(), l->d.warp_desc, W,        \
-                                                 l->d.row_map, l->info.nznrows, n, v.p, v.q, scal, sc.partials,    \
-                                                 sc.gsum, sc.gcnt, e->scale.as<float>())
+  k_spmv_dot<V, X, M, D><<<g, CG_BLOCK, smem, st>>>(                                                                \
+      e->vals.as<V>(), e->cols.as<int32_t>(), e->c16.as<uint16_t>(), e->c32.as<int32_t>(), e->cdesc.as<int4>(),     \
+      l->d.warp_desc, W, l->d.row_map, l->info.nznrows, n, v.p, v.q, scal, sc.partials, sc.gsum, sc.gcnt,           \
+      e->scale.as<float>(), e->w16.as<uint16_t>(), e->wchunks.as<int2>(), e->wdesc.as<int4>())
 #define WK_SPMV_DOT1(V, M)                                                                                          \
   do {                                                                                                              \
     if (d64) WK_SPMV_DOT2(V, M, true); else WK_SPMV_DOT2(V, M, false);                                              \
   } while (0)
 #define WK_SPMV_DOT(V)                                                                                              \
   do {                                                                                                              \
-    if (mode == 2) WK_SPMV_DOT1(V, 2); else if (mode == 1) WK_SPMV_DOT1(V, 1); else WK_SPMV_DOT1(V, 0);             \
+    if (mode == 2) WK_SPMV_DOT1(V, 2); else if (mode == 1) WK_SPMV_DOT1(V, 1);                                      \
+    else if (mode == 3) WK_SPMV_DOT1(V, 3); else WK_SPMV_DOT1(V, 0);                                                \
   } while (0)
   if constexpr (sizeof(X) == 8) {
     WK_SPMV_DOT(double);
