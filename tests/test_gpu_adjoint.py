@@ -428,3 +428,53 @@ def test_fp32_slot_order_at_benchmark_size_hex64():
     rp_d, cols_d, vals_d = fe.fe_matrix(3, 64, 64, 64, 3, 1, 4)
     rp, cols, vals = rp_d.cpu().numpy(), cols_d.cpu().numpy(), vals_d.cpu().numpy()
     _check_fp32_slot_gradient(rp, cols, vals, 2, 81, np.random.default_rng(64))
+
+
+def test_fp32_slot_order_gradient_alone_and_unsymmetric_patterns():
+    """The value gradient without dx (any pattern) and the unsymmetric
+    patterns' gradient in fp32 slot order run the staged kernel's
+    gradient-only form: dvals bit-identical to the FP32 products dy[row]
+    x[col], padding slots 0, the same bits as the full adjoint of a symmetric
+    pattern; dx (from A^T's SpMV) within 1e-5 of the host transpose."""
+    import torch
+
+    from warpkernel_gb300.autograd import WPKMatrix
+    rng = np.random.default_rng(31)
+    # unsymmetric: a random pattern, and an FE matrix with 1 % of its
+    # off-diagonal entries dropped (most warps keep an x window)
+    rp_f, cols_f, vals_f = O.fe_matrix(3, 10, 10, 10, 3, value_mode=1, seed=8)
+    rows_f = np.repeat(np.arange(len(rp_f) - 1), np.diff(rp_f))
+    keep = (rows_f == cols_f) | (rng.random(len(cols_f)) > 0.01)
+    rp_k = np.zeros(len(rp_f), np.int64)
+    np.add.at(rp_k, rows_f[keep] + 1, 1)
+    cases = [(random_csr(rng, 5000, 60, p_empty=0.05), 7),
+             ((np.cumsum(rp_k).astype(np.int32), cols_f[keep], vals_f[keep]), 81)]
+    for (rp, cols, vals), th in cases:
+        n = len(rp) - 1
+        rows = np.repeat(np.arange(n), np.diff(rp))
+        vh = vals.astype(np.float32)
+        xh = rng.uniform(-1, 1, n).astype(np.float32)
+        dyh = rng.uniform(-1, 1, n).astype(np.float32)
+        m_csr = WPKMatrix(rp, cols, torch.from_numpy(vh), kind=2, threshold=th)
+        assert not m_csr.symmetric
+        mat = WPKMatrix(rp, cols, m_csr.to_slots(torch.from_numpy(vh).cuda()), kind=2, threshold=th,
+                        value_order="slots")
+        dx, dv = mat.adjoint(torch.from_numpy(xh).cuda(), torch.from_numpy(dyh).cuda())
+        pad = torch.ones(mat.allocate_nz, dtype=torch.bool, device="cuda")
+        pad[mat._reorder_rows()] = False
+        assert not torch.any(dv[pad] != 0)
+        assert np.array_equal(mat.to_csr(dv).cpu().numpy(), dyh[rows] * xh[cols])
+        dx_ref = O.csr_spmv_t(rp, cols, vh.astype(np.float64), dyh.astype(np.float64), n)
+        assert rel(dx.double().cpu().numpy(), dx_ref) < 1e-5
+    # a symmetric band: the gradient alone against the full adjoint's
+    rp, cols = _periodic_band(3000, 27)
+    vals = rng.standard_normal(len(cols)).astype(np.float32)
+    m_csr = WPKMatrix(rp, cols, torch.from_numpy(vals), kind=2, threshold=27)
+    mat = WPKMatrix(rp, cols, m_csr.to_slots(torch.from_numpy(vals).cuda()), kind=2, threshold=27,
+                    value_order="slots")
+    assert mat.symmetric
+    x = torch.from_numpy(rng.uniform(-1, 1, 3000).astype(np.float32)).cuda()
+    dy = torch.from_numpy(rng.uniform(-1, 1, 3000).astype(np.float32)).cuda()
+    _, dv_full = mat.adjoint(x, dy)
+    dx_none, dv_alone = mat.adjoint(x, dy, want_dx=False, want_dvals=True)
+    assert dx_none is None and torch.equal(dv_alone, dv_full)

@@ -147,7 +147,7 @@ __global__ void k_dvals_slots(const int4 *__restrict__ desc, uint32_t W, const i
 // with one vector store per lane, or (CSR order) through shared memory, which
 // measured 11 % faster (fp32) than the 4-slot kernel it replaced.  It serves
 // fp64 and CSR order; the fp32 slot-order gradient runs k_adjoint_sym_staged
-// (below), 0.114 against 0.1415 ms at hex 64^3.  For fp64 this kernel stayed
+// (below), 0.105 against 0.1415 ms at hex 64^3.  For fp64 this kernel stayed
 // ahead of a register-staged form of that kernel (0.262 against 0.264 ms,
 // 0.289 with x windows).
 template <typename T>
@@ -439,8 +439,10 @@ constexpr int ADJ_SW = 4;  // warps per block
 // are known, before the row data and the window, which join the first
 // group.  WIN: the warp has an x window (its (x, dy) pairs staged in `wp`,
 // the stream carries 16-bit window positions); otherwise the stream carries
-// 32-bit columns and x, dy are gathered from their vectors.
-template <int STAGES, bool WIN>
+// 32-bit columns and x, dy are gathered from their vectors.  DX = false:
+// the value gradient alone (no mirror values streamed, no dx; the window
+// holds x only).
+template <int STAGES, bool WIN, bool DX = true>
 __device__ __forceinline__ float adjoint_warp_pipe(const int4 d, const int4 wd, const int2 *__restrict__ wch,
                                                    const int32_t *__restrict__ pc, const uint16_t *__restrict__ w16,
                                                    const float *__restrict__ tv, const float *__restrict__ x,
@@ -460,9 +462,11 @@ __device__ __forceinline__ float adjoint_warp_pipe(const int4 d, const int4 wd, 
   auto issue = [&](uint32_t u) {
     if (u < full || lane < 4 * rem) {
       const size_t g = o + (size_t)u * S * WS + S * lane;
-      uint32_t *dv = sv + (u % STAGES) * VSTAGE + S * lane;
+      if constexpr (DX) {
+        uint32_t *dv = sv + (u % STAGES) * VSTAGE + S * lane;
 #pragma unroll
-      for (int q = 0; q < S; q += 4) cp_async16(dv + q, tv + g + q, pol);
+        for (int q = 0; q < S; q += 4) cp_async16(dv + q, tv + g + q, pol);
+      }
       uint32_t *dc = sc + (u % STAGES) * CSTAGE + NC * lane;
       const uint32_t *gc =
           WIN ? reinterpret_cast<const uint32_t *>(w16 + g) : reinterpret_cast<const uint32_t *>(pc + g);
@@ -495,7 +499,7 @@ __device__ __forceinline__ float adjoint_warp_pipe(const int4 d, const int4 wd, 
       const int pos = (pl & 0xffff) + (int)lane;
       if (lane < (uint32_t)(pl >> 16) && pos < WIN_MAX) {
         cp_async_ca<4>(&wp[pos].x, x + c0 + (int)lane);
-        cp_async_ca<4>(&wp[pos].y, dy + c0 + (int)lane);
+        if constexpr (DX) cp_async_ca<4>(&wp[pos].y, dy + c0 + (int)lane);
       }
     }
   }
@@ -515,15 +519,14 @@ __device__ __forceinline__ float adjoint_warp_pipe(const int4 d, const int4 wd, 
     float *dp = dvals + o + (size_t)u * S * WS + lane;
     auto step = [&](int st) {
       const int q = st * WS + (int)lane;
-      const float v = __uint_as_float(svs[q]);
       float2 g;
       if constexpr (WIN) {
         g = wp[reinterpret_cast<const uint16_t *>(scs)[q]];
       } else {
         const int c = (int)scs[q];
-        g = make_float2(__ldg(x + c), __ldg(dy + c));
+        g = make_float2(__ldg(x + c), DX ? __ldg(dy + c) : 0.f);
       }
-      acc = fmaf(v, g.y, acc);
+      if constexpr (DX) acc = fmaf(__uint_as_float(svs[q]), g.y, acc);
       __stcs(dp + st * WS, (int)(u * S + st) < el ? dyr * g.x : 0.f);
     };
     if (u < full) {  // a full unit: no guards, so the tile reads can be batched
@@ -539,8 +542,9 @@ __device__ __forceinline__ float adjoint_warp_pipe(const int4 d, const int4 wd, 
 }
 
 // STAGES tiles in the ring, BLOCKS blocks per SM.  ALLWIN: every warp has
-// an x window, so the column tiles hold 16-bit positions only.
-template <int STAGES, int BLOCKS, bool ALLWIN>
+// an x window, so the column tiles hold 16-bit positions only.  DX = false:
+// dvals alone (any pattern: no mirror values, dx untouched).
+template <int STAGES, int BLOCKS, bool ALLWIN, bool DX = true>
 __global__ void __launch_bounds__(ADJ_SW * 32, BLOCKS) k_adjoint_sym_staged(
     const int4 *__restrict__ desc, uint32_t W, const int32_t *__restrict__ row_map, const uint32_t *__restrict__ slen,
     uint32_t nzr, uint32_t nrows, const int32_t *__restrict__ pc, const uint16_t *__restrict__ w16,
@@ -549,7 +553,7 @@ __global__ void __launch_bounds__(ADJ_SW * 32, BLOCKS) k_adjoint_sym_staged(
   using namespace core;
   constexpr int S = 8;
   constexpr int NCW = ALLWIN ? S / 2 : S;  // column words per lane and unit
-  __shared__ __align__(16) uint32_t s_val[ADJ_SW][STAGES * S * WS];
+  __shared__ __align__(16) uint32_t s_val[ADJ_SW][DX ? STAGES * S * WS : 4];
   __shared__ __align__(16) uint32_t s_col[ADJ_SW][STAGES * NCW * WS];
   __shared__ __align__(16) float2 s_win[ADJ_SW][WIN_MAX];
   const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x / WS;
@@ -559,22 +563,25 @@ __global__ void __launch_bounds__(ADJ_SW * 32, BLOCKS) k_adjoint_sym_staged(
     const int4 d = desc[w], wd = wdesc[w];  // independent loads, in flight together
     int32_t row;
     bool valid;
-    float acc;
+    float acc = 0.f;
     if (ALLWIN || wd.y != 0) {
-      acc = adjoint_warp_pipe<STAGES, true>(d, wd, wch, pc, w16, tv, x, dy, row_map, slen, nzr, s_win[wib], dvals,
-                                            s_val[wib], s_col[wib], lane, pol, row, valid);
+      acc = adjoint_warp_pipe<STAGES, true, DX>(d, wd, wch, pc, w16, tv, x, dy, row_map, slen, nzr, s_win[wib],
+                                                dvals, s_val[wib], s_col[wib], lane, pol, row, valid);
     } else {
       if constexpr (!ALLWIN)
-        acc = adjoint_warp_pipe<STAGES, false>(d, wd, wch, pc, w16, tv, x, dy, row_map, slen, nzr, nullptr, dvals,
-                                               s_val[wib], s_col[wib], lane, pol, row, valid);
+        acc = adjoint_warp_pipe<STAGES, false, DX>(d, wd, wch, pc, w16, tv, x, dy, row_map, slen, nzr, nullptr,
+                                                   dvals, s_val[wib], s_col[wib], lane, pol, row, valid);
     }
-    const uint32_t T_ = (uint32_t)d.z;
-    for (uint32_t k = 1; k < T_; k <<= 1) acc += __shfl_down_sync(0xffffffffu, acc, k);
-    if (valid && (lane & (T_ - 1)) == 0) dx[row] = acc;
+    if constexpr (DX) {
+      const uint32_t T_ = (uint32_t)d.z;
+      for (uint32_t k = 1; k < T_; k <<= 1) acc += __shfl_down_sync(0xffffffffu, acc, k);
+      if (valid && (lane & (T_ - 1)) == 0) dx[row] = acc;
+    }
   }
-  for (size_t q = (size_t)nzr + (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < nrows;
-       q += (size_t)gridDim.x * blockDim.x)
-    dx[row_map[q]] = 0.f;
+  if constexpr (DX)
+    for (size_t q = (size_t)nzr + (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < nrows;
+         q += (size_t)gridDim.x * blockDim.x)
+      dx[row_map[q]] = 0.f;
 }
 
 wk_status refresh_transposed(wk_adjoint *a, const void *vals_csr, cudaStream_t st) {
@@ -802,7 +809,26 @@ extern "C" wk_status wk_adjoint_run(wk_adjoint *a, const void *x, const void *dy
     RunArgs ra{a->te, 0, 0, 1, WK_ORDER_FAST, true, dy, dx, st};
     WK_TRY(launch_spmv(ra));
   }
-  if (dvals && W) {
+  if (dvals && W && !f64 && slots) {
+    // fp32 gradient in slot order: the staged kernel without mirror values or
+    // dx, gathering x from the layout warps' windows
+    if (!a->win_built) {
+      WK_TRY(build_window_set(L, f->cols.as<int32_t>(), a->win, st));
+      a->win_built = true;
+    }
+    const unsigned g = (unsigned)std::max<size_t>(1, ((size_t)W + ADJ_SW - 1) / ADJ_SW);
+#define WK_ADJ_DV(AW)                                                                                              \
+  k_adjoint_sym_staged<4, 6, AW, false><<<g, ADJ_SW * 32, 0, st>>>(                                                \
+      L->d.warp_desc, W, L->d.row_map, L->d.slen, L->info.nznrows, n, f->cols.as<int32_t>(),                      \
+      a->win.w16.as<uint16_t>(), a->win.chunks.as<int2>(), a->win.wdesc.as<int4>(), nullptr, (const float *)x,    \
+      (const float *)dy, nullptr, (float *)dvals)
+    if (a->win.warps == W)
+      WK_ADJ_DV(true);
+    else
+      WK_ADJ_DV(false);
+#undef WK_ADJ_DV
+    WK_CHECK_LAUNCH();
+  } else if (dvals && W) {
     const unsigned g = (unsigned)std::max<size_t>(1, ((size_t)W * WS + 255) / 256);
 #define WK_DV(T)                                                                                                       \
   do {                                                                                                                 \
