@@ -146,8 +146,9 @@ __global__ void k_dvals_slots(const int4 *__restrict__ desc, uint32_t W, const i
 // 128-bit accesses despite the lower occupancy).  dvals go to the same slots
 // with one vector store per lane, or (CSR order) through shared memory, which
 // measured 11 % faster (fp32) than the 4-slot kernel it replaced.  It serves
-// fp64 and CSR order; the fp32 slot-order gradient runs k_adjoint_sym_staged
-// (below), 0.105 against 0.1415 ms at hex 64^3.  For fp64 this kernel stayed
+// fp64; the fp32 gradient runs k_adjoint_sym_staged (slot order, 0.105
+// against 0.1415 ms at hex 64^3) or k_adjoint_sym_staged_csr (CSR order,
+// 0.1755 against 0.207 ms).  For fp64 this kernel stayed
 // ahead of a register-staged form of that kernel (0.262 against 0.264 ms,
 // 0.289 with x windows).
 template <typename T>
@@ -193,6 +194,22 @@ __device__ __forceinline__ void flush_csr_chunk(T *__restrict__ dvals, const T (
 #pragma unroll 4
   for (uint32_t sg = 0; sg < 32; sg += 32 / ADJ_CSR_CHUNK) {
     const uint32_t l = sg + lane / ADJ_CSR_CHUNK;
+    const uint32_t e = c0 + jj;
+    if (jj < nst && (int)e < sel[l]) __stcs(dvals + (size_t)skb[l] + e, stg[l][jj]);
+  }
+  __syncwarp();
+}
+
+// The same with an explicit chunk CH (16 or 32 steps; stg rows of CH + 1).
+template <int CH>
+__device__ __forceinline__ void flush_csr_chunk_n(float *__restrict__ dvals, const float (*stg)[CH + 1],
+                                                  const int *__restrict__ skb, const int *__restrict__ sel,
+                                                  uint32_t c0, uint32_t nst, uint32_t lane) {
+  __syncwarp();
+  const uint32_t jj = lane % CH;
+#pragma unroll 4
+  for (uint32_t sg = 0; sg < 32; sg += 32 / CH) {
+    const uint32_t l = sg + lane / CH;
     const uint32_t e = c0 + jj;
     if (jj < nst && (int)e < sel[l]) __stcs(dvals + (size_t)skb[l] + e, stg[l][jj]);
   }
@@ -441,15 +458,24 @@ constexpr int ADJ_SW = 4;  // warps per block
 // the stream carries 16-bit window positions); otherwise the stream carries
 // 32-bit columns and x, dy are gathered from their vectors.  DX = false:
 // the value gradient alone (no mirror values streamed, no dx; the window
-// holds x only).
-template <int STAGES, bool WIN, bool DX = true>
+// holds x only).  CSR: dvals in CSR order (`cs`: the warp's staging of
+// ADJ_CSR_STAGED-step chunks as [layout lane][step], flushed row segment by
+// row segment).
+constexpr int ADJ_CSR_STAGED = 32;  // hex 64^3: 0.1755 ms; 16-step chunks (half-warp row segments) 0.181
+struct CsrStage {
+  float (*stg)[ADJ_CSR_STAGED + 1];
+  int *skb, *sel;
+  const int32_t *rowptr;
+};
+template <int STAGES, bool WIN, bool DX = true, bool CSR = false>
 __device__ __forceinline__ float adjoint_warp_pipe(const int4 d, const int4 wd, const int2 *__restrict__ wch,
                                                    const int32_t *__restrict__ pc, const uint16_t *__restrict__ w16,
                                                    const float *__restrict__ tv, const float *__restrict__ x,
                                                    const float *__restrict__ dy, const int32_t *__restrict__ row_map,
                                                    const uint32_t *__restrict__ slen, uint32_t nzr, float2 *wp,
                                                    float *__restrict__ dvals, uint32_t *sv, uint32_t *sc,
-                                                   uint32_t lane, uint64_t pol, int32_t &row, bool &valid) {
+                                                   uint32_t lane, uint64_t pol, int32_t &row, bool &valid,
+                                                   const CsrStage cs = CsrStage{}) {
   using namespace core;
   constexpr int S = 8;                 // steps per unit (32 bytes of fp32 per lane)
   constexpr int NC = WIN ? S / 2 : S;  // column words per lane and unit
@@ -489,6 +515,10 @@ __device__ __forceinline__ float adjoint_warp_pipe(const int4 d, const int4 wd, 
     el = max(0, min((int)A, (int)slen[p] - (int)(t * A)));
     dyr = dy[row];
   }
+  if constexpr (CSR) {  // the lane's first CSR entry and entry count, for the flushes
+    cs.skb[lane] = valid ? cs.rowptr[row] + (int)(t * A) : 0;
+    cs.sel[lane] = el;
+  }
   if constexpr (WIN) {
     // chunk q = {first column, window position | length << 16}, <= 32 columns
     const int nch = wd.y;
@@ -527,17 +557,29 @@ __device__ __forceinline__ float adjoint_warp_pipe(const int4 d, const int4 wd, 
         g = make_float2(__ldg(x + c), DX ? __ldg(dy + c) : 0.f);
       }
       if constexpr (DX) acc = fmaf(__uint_as_float(svs[q]), g.y, acc);
-      __stcs(dp + st * WS, (int)(u * S + st) < el ? dyr * g.x : 0.f);
+      const float gv = (int)(u * S + st) < el ? dyr * g.x : 0.f;
+      if constexpr (CSR)
+        cs.stg[lane][(u * S + st) % ADJ_CSR_STAGED] = gv;
+      else
+        __stcs(dp + st * WS, gv);
     };
     if (u < full) {  // a full unit: no guards, so the tile reads can be batched
 #pragma unroll
       for (int st = 0; st < S; st++) step(st);
+      if constexpr (CSR)
+        if (((u + 1) * S) % ADJ_CSR_STAGED == 0)
+          flush_csr_chunk_n<ADJ_CSR_STAGED>(dvals, cs.stg, cs.skb, cs.sel, (u + 1) * S - ADJ_CSR_STAGED,
+                                            ADJ_CSR_STAGED, lane);
     } else {
       for (int st = 0; st < (int)rem; st++) step(st);
     }
     __syncwarp();  // this tile is refilled STAGES - 1 units later
   }
   cp_async_wait<0>();
+  if constexpr (CSR) {  // the last, partial chunk
+    const uint32_t c0 = A / ADJ_CSR_STAGED * ADJ_CSR_STAGED;
+    if (A > c0) flush_csr_chunk_n<ADJ_CSR_STAGED>(dvals, cs.stg, cs.skb, cs.sel, c0, A - c0, lane);
+  }
   return acc;
 }
 
@@ -582,6 +624,61 @@ __global__ void __launch_bounds__(ADJ_SW * 32, BLOCKS) k_adjoint_sym_staged(
     for (size_t q = (size_t)nzr + (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < nrows;
          q += (size_t)gridDim.x * blockDim.x)
       dx[row_map[q]] = 0.f;
+}
+
+// The fused adjoint with dvals in CSR order: the staged kernel's pipe with
+// each warp's 32-step chunks of gradients staged as [layout lane][step] and
+// written row segment by row segment.  Shared memory per warp (dynamic):
+// STAGES value and column tiles, the x window, the staging and the lanes'
+// CSR offsets and entry counts.
+template <int STAGES, bool ALLWIN>
+struct AdjCsrCfg {
+  static constexpr int S = 8, NCW = ALLWIN ? S / 2 : S;
+  static constexpr int V_WORDS = STAGES * S * WS, C_WORDS = STAGES * NCW * WS, WIN_WORDS = WIN_MAX * 2;
+  static constexpr int STG_WORDS = (32 * (ADJ_CSR_STAGED + 1) + 3) / 4 * 4;
+  static constexpr int WARP_WORDS = V_WORDS + C_WORDS + WIN_WORDS + STG_WORDS + 64;
+  static constexpr size_t SMEM = (size_t)ADJ_SW * WARP_WORDS * 4;
+};
+
+template <int STAGES, bool ALLWIN>
+__global__ void __launch_bounds__(ADJ_SW * 32) k_adjoint_sym_staged_csr(
+    const int4 *__restrict__ desc, uint32_t W, const int32_t *__restrict__ row_map, const uint32_t *__restrict__ slen,
+    const int32_t *__restrict__ rowptr, uint32_t nzr, uint32_t nrows, const int32_t *__restrict__ pc,
+    const uint16_t *__restrict__ w16, const int2 *__restrict__ wch, const int4 *__restrict__ wdesc,
+    const float *__restrict__ tv, const float *__restrict__ x, const float *__restrict__ dy, float *__restrict__ dx,
+    float *__restrict__ dvals) {
+  using namespace core;
+  using C = AdjCsrCfg<STAGES, ALLWIN>;
+  extern __shared__ __align__(16) uint32_t adj_csr_smem[];
+  const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x / WS;
+  uint32_t *base = adj_csr_smem + wib * C::WARP_WORDS;
+  uint32_t *sv = base, *sc = base + C::V_WORDS;
+  float2 *wp = reinterpret_cast<float2 *>(sc + C::C_WORDS);
+  float(*stg)[ADJ_CSR_STAGED + 1] = reinterpret_cast<float(*)[ADJ_CSR_STAGED + 1]>(sc + C::C_WORDS + C::WIN_WORDS);
+  int *skb = reinterpret_cast<int *>(sc + C::C_WORDS + C::WIN_WORDS + C::STG_WORDS);
+  const CsrStage cs{stg, skb, skb + 32, rowptr};
+  const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) / WS;
+  if (w < W) {
+    const uint64_t pol = policy_evict_first();
+    const int4 d = desc[w], wd = wdesc[w];
+    int32_t row;
+    bool valid;
+    float acc = 0.f;
+    if (ALLWIN || wd.y != 0) {
+      acc = adjoint_warp_pipe<STAGES, true, true, true>(d, wd, wch, pc, w16, tv, x, dy, row_map, slen, nzr, wp,
+                                                        dvals, sv, sc, lane, pol, row, valid, cs);
+    } else {
+      if constexpr (!ALLWIN)
+        acc = adjoint_warp_pipe<STAGES, false, true, true>(d, wd, wch, pc, w16, tv, x, dy, row_map, slen, nzr,
+                                                           nullptr, dvals, sv, sc, lane, pol, row, valid, cs);
+    }
+    const uint32_t T_ = (uint32_t)d.z;
+    for (uint32_t k = 1; k < T_; k <<= 1) acc += __shfl_down_sync(0xffffffffu, acc, k);
+    if (valid && (lane & (T_ - 1)) == 0) dx[row] = acc;
+  }
+  for (size_t q = (size_t)nzr + (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < nrows;
+       q += (size_t)gridDim.x * blockDim.x)
+    dx[row_map[q]] = 0.f;
 }
 
 wk_status refresh_transposed(wk_adjoint *a, const void *vals_csr, cudaStream_t st) {
@@ -772,6 +869,34 @@ extern "C" wk_status wk_adjoint_run(wk_adjoint *a, const void *x, const void *dy
       else
         WK_ADJ_ST(4, 4, false);
 #undef WK_ADJ_ST
+      WK_CHECK_LAUNCH();
+      return WK_OK;
+    }
+    // fp32 gradient in CSR order: the same pipe, gradients staged per warp
+    // and written row segment by row segment; two stages leave four blocks
+    // per SM (hex 64^3: 0.1755 ms, three stages 0.183, k_adjoint_sym_slots
+    // 0.207)
+    if (!f64) {
+      if (!a->win_built) {
+        WK_TRY(build_window_set(L, f->cols.as<int32_t>(), a->win, st));
+        a->win_built = true;
+      }
+      const unsigned g = (unsigned)std::max<size_t>(1, ((size_t)W + ADJ_SW - 1) / ADJ_SW);
+#define WK_ADJ_CSR(ST, AW)                                                                                         \
+  do {                                                                                                             \
+    const size_t sm = AdjCsrCfg<ST, AW>::SMEM;                                                                     \
+    WK_CUDA(cudaFuncSetAttribute(k_adjoint_sym_staged_csr<ST, AW>, cudaFuncAttributeMaxDynamicSharedMemorySize,    \
+                                 (int)sm));                                                                        \
+    k_adjoint_sym_staged_csr<ST, AW><<<g, ADJ_SW * 32, sm, st>>>(                                                  \
+        L->d.warp_desc, W, L->d.row_map, L->d.slen, L->d.rowptr, L->info.nznrows, n, f->cols.as<int32_t>(),        \
+        a->win.w16.as<uint16_t>(), a->win.chunks.as<int2>(), a->win.wdesc.as<int4>(), a->te->vals.as<float>(),    \
+        (const float *)x, (const float *)dy, (float *)dx, (float *)dvals);                                         \
+  } while (0)
+      if (a->win.warps == W)
+        WK_ADJ_CSR(2, true);
+      else
+        WK_ADJ_CSR(2, false);
+#undef WK_ADJ_CSR
       WK_CHECK_LAUNCH();
       return WK_OK;
     }
