@@ -200,18 +200,21 @@ __device__ __forceinline__ void flush_csr_chunk(T *__restrict__ dvals, const T (
   __syncwarp();
 }
 
-// The same with an explicit chunk CH (16 or 32 steps; stg rows of CH + 1).
-template <int CH>
-__device__ __forceinline__ void flush_csr_chunk_n(float *__restrict__ dvals, const float (*stg)[CH + 1],
+// The same for the staged kernel's 32-step chunks: each lane computes its
+// own row's store limit and CSR offset for the chunk once, and the loop over
+// rows takes them by shuffle (two shuffles, one compare and one store per
+// row segment).
+__device__ __forceinline__ void flush_csr_chunk32(float *__restrict__ dvals, const float (*stg)[33],
                                                   const int *__restrict__ skb, const int *__restrict__ sel,
                                                   uint32_t c0, uint32_t nst, uint32_t lane) {
   __syncwarp();
-  const uint32_t jj = lane % CH;
-#pragma unroll 4
-  for (uint32_t sg = 0; sg < 32; sg += 32 / CH) {
-    const uint32_t l = sg + lane / CH;
-    const uint32_t e = c0 + jj;
-    if (jj < nst && (int)e < sel[l]) __stcs(dvals + (size_t)skb[l] + e, stg[l][jj]);
+  const int lim_me = min((int)nst, sel[lane] - (int)c0);  // entries of this lane's row in the chunk
+  const int off_me = skb[lane] + (int)c0;
+#pragma unroll 8
+  for (int l = 0; l < 32; l++) {
+    const int lim = __shfl_sync(0xffffffffu, lim_me, l);
+    const int off = __shfl_sync(0xffffffffu, off_me, l);
+    if ((int)lane < lim) __stcs(dvals + (uint32_t)(off + (int)lane), stg[l][lane]);
   }
   __syncwarp();
 }
@@ -568,8 +571,7 @@ __device__ __forceinline__ float adjoint_warp_pipe(const int4 d, const int4 wd, 
       for (int st = 0; st < S; st++) step(st);
       if constexpr (CSR)
         if (((u + 1) * S) % ADJ_CSR_STAGED == 0)
-          flush_csr_chunk_n<ADJ_CSR_STAGED>(dvals, cs.stg, cs.skb, cs.sel, (u + 1) * S - ADJ_CSR_STAGED,
-                                            ADJ_CSR_STAGED, lane);
+          flush_csr_chunk32(dvals, cs.stg, cs.skb, cs.sel, (u + 1) * S - ADJ_CSR_STAGED, ADJ_CSR_STAGED, lane);
     } else {
       for (int st = 0; st < (int)rem; st++) step(st);
     }
@@ -578,7 +580,7 @@ __device__ __forceinline__ float adjoint_warp_pipe(const int4 d, const int4 wd, 
   cp_async_wait<0>();
   if constexpr (CSR) {  // the last, partial chunk
     const uint32_t c0 = A / ADJ_CSR_STAGED * ADJ_CSR_STAGED;
-    if (A > c0) flush_csr_chunk_n<ADJ_CSR_STAGED>(dvals, cs.stg, cs.skb, cs.sel, c0, A - c0, lane);
+    if (A > c0) flush_csr_chunk32(dvals, cs.stg, cs.skb, cs.sel, c0, A - c0, lane);
   }
   return acc;
 }
