@@ -148,7 +148,7 @@ __global__ void k_dvals_slots(const int4 *__restrict__ desc, uint32_t W, const i
 // measured 11 % faster (fp32) than the 4-slot kernel it replaced.  It serves
 // fp64; the fp32 gradient runs k_adjoint_sym_staged (slot order, 0.105
 // against 0.1415 ms at hex 64^3) or k_adjoint_sym_staged_csr (CSR order,
-// 0.1755 against 0.207 ms).  For fp64 this kernel stayed
+// 0.1584 against 0.207 ms).  For fp64 this kernel stayed
 // ahead of a register-staged form of that kernel (0.262 against 0.264 ms,
 // 0.289 with x windows).
 template <typename T>
@@ -464,7 +464,7 @@ constexpr int ADJ_SW = 4;  // warps per block
 // holds x only).  CSR: dvals in CSR order (`cs`: the warp's staging of
 // ADJ_CSR_STAGED-step chunks as [layout lane][step], flushed row segment by
 // row segment).
-constexpr int ADJ_CSR_STAGED = 32;  // hex 64^3: 0.1755 ms; 16-step chunks (half-warp row segments) 0.181
+constexpr int ADJ_CSR_STAGED = 32;  // 16-step chunks (half-warp row segments) measured slower
 struct CsrStage {
   float (*stg)[ADJ_CSR_STAGED + 1];
   int *skb, *sel;
@@ -876,7 +876,7 @@ extern "C" wk_status wk_adjoint_run(wk_adjoint *a, const void *x, const void *dy
     }
     // fp32 gradient in CSR order: the same pipe, gradients staged per warp
     // and written row segment by row segment; two stages leave four blocks
-    // per SM (hex 64^3: 0.1755 ms, three stages 0.183, k_adjoint_sym_slots
+    // per SM (hex 64^3: 0.1584 ms, three stages 0.1582, k_adjoint_sym_slots
     // 0.207)
     if (!f64) {
       if (!a->win_built) {
